@@ -1,0 +1,199 @@
+/*
+ * gbpowspec.h -- C ABI of libgbpowspec.so, the GB300 power-spectrum engine.
+ *
+ * The library replaces the particle -> mesh -> P_l(k) path of jax-powspec
+ * (dforero0896/jax-powspec).  Each entry point below names the reference
+ * function it stands in for (path within the reference project, file:line).
+ *
+ * Conventions shared by every call
+ *   - All array arguments are DEVICE pointers owned by the caller; the library
+ *     never frees them.  Scratch memory is passed in as (workspace, bytes);
+ *     the matching *_workspace_size call says how much is needed.
+ *   - Every call is asynchronous on the given stream and returns GBP_OK (0)
+ *     or a negative status; gbp_strerror() turns it into text.  Argument
+ *     errors are detected on the host before anything is launched.
+ *   - Meshes are float32, C order [x][y][z] (z fastest), side n_mesh.
+ *     Interlaced deposits write two meshes back to back: grid 0 at mesh_out,
+ *     grid 1 (particles shifted by +half a cell on every axis) at
+ *     mesh_out + n_mesh^3.
+ *   - Spectra are complex64 [x][y][z] with n_mesh/2+1 entries along z (the
+ *     cuFFT real-to-complex layout), one per grid, back to back.
+ *   - Results are deterministic: the same inputs give bitwise-identical
+ *     outputs on every run, whatever else shares the GPU.
+ */
+#ifndef GBPOWSPEC_H
+#define GBPOWSPEC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* cudaStream_t without pulling in the CUDA headers. */
+typedef struct CUstream_st* gbp_stream_t;
+
+/* status codes */
+#define GBP_OK                 0
+#define GBP_ERR_INVALID       -1  /* bad argument (detected on the host) */
+#define GBP_ERR_CUDA          -2  /* a CUDA runtime call failed */
+#define GBP_ERR_CUFFT         -3  /* a cuFFT call failed */
+#define GBP_ERR_WORKSPACE     -4  /* workspace smaller than *_workspace_size */
+#define GBP_ERR_UNSUPPORTED   -5  /* valid request outside what this build supports */
+#define GBP_ERR_ALLOC         -6  /* the library could not allocate plan memory */
+
+/* mass-assignment schemes (B-spline order) */
+#define GBP_NGP 1
+#define GBP_CIC 2
+#define GBP_TSC 3
+#define GBP_PCS 4
+
+/* deposit semantics */
+#define GBP_COMPAT_NONE    0  /* periodic B-spline deposit (mass conserving)        */
+#define GBP_COMPAT_VEC     1  /* exactly src/mas.py cic_mas_vec, bugs included      */
+#define GBP_COMPAT_SCAN    2  /* exactly src/mas.py cic_mas, bugs included          */
+
+/* multipole selection for gbp_power */
+#define GBP_ELL0   1
+#define GBP_ELL2   2
+#define GBP_ELL4   4
+#define GBP_KSUM   8   /* also accumulate sum of |k| per bin (mode-averaged k) */
+
+const char* gbp_strerror(int status);
+int gbp_version(void);
+
+/* ------------------------------------------------------------------------
+ * Deposit: particles -> density mesh(es).
+ * Replaces src/mas.py:88-153 (cic_mas_vec) for compat == GBP_COMPAT_VEC and
+ * src/mas.py:5-87 (cic_mas) for compat == GBP_COMPAT_SCAN; with
+ * GBP_COMPAT_NONE it adds NGP/TSC/PCS and interlacing (no reference code).
+ *
+ *   x,y,z        float32[n] positions; w float32[n] weights or NULL (= 1).
+ *   xmin,ymin,zmin  mesh origin; inv_cell = float32 (1 / (box/n_mesh)),
+ *                computed by the caller exactly as src/mas.py:100-101 does.
+ *   mas          GBP_NGP..GBP_PCS (compat modes require GBP_CIC).
+ *   interlace    0/1: also deposit the half-cell-shifted grid.
+ *   wrap         compat modes only: the reference's `wrap` flag.
+ *   mesh_in      NULL, or float32 mesh(es) to which the deposit is added
+ *                (src/mas.py returns delta + deposits).
+ *   mesh_out     float32 [1+interlace][n_mesh^3]; fully overwritten.
+ *   stats_out    NULL or device gbp_deposit_stats (written by the call).
+ * Accumulation is exact fixed point (int64, scale 2^s chosen from n and
+ * max|w|), so the result does not depend on particle order or scheduling.
+ * ---------------------------------------------------------------------- */
+typedef struct gbp_deposit_stats {
+  double mass[2];       /* sum of the deposited mesh, per grid              */
+  double sum_w;         /* sum of weights of the particles that were kept   */
+  double sum_w2;        /* sum of squared weights (shot noise)              */
+  long long n_kept;     /* particles that deposited at least one cell       */
+  long long n_nonfinite;/* particles dropped for a non-finite coordinate    */
+  int scale_exp;        /* fixed-point exponent s used by the accumulation  */
+  int pad_;
+} gbp_deposit_stats;
+
+int gbp_deposit_workspace_size(int64_t n_particles, int n_mesh, int mas,
+                               int interlace, int compat, size_t* bytes);
+
+int gbp_deposit(const float* x, const float* y, const float* z, const float* w,
+                int64_t n_particles, float xmin, float ymin, float zmin,
+                float inv_cell, int n_mesh, int mas, int interlace, int compat,
+                int wrap, const float* mesh_in, float* mesh_out,
+                gbp_deposit_stats* stats_out, void* workspace,
+                size_t workspace_bytes, gbp_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * FFT plans: a cached cuFFT 3D real-to-complex plan for n_grids meshes of
+ * side n_mesh.  Replaces the jnp.fft.rfftn of src/correlations.py:22.
+ * The plan does not own a work area; gbp_fft_r2c takes one.
+ * ---------------------------------------------------------------------- */
+typedef struct gbp_fft_plan_s* gbp_fft_plan;
+
+int gbp_fft_plan_create(int n_mesh, int n_grids, gbp_fft_plan* plan,
+                        size_t* workspace_bytes);
+int gbp_fft_plan_destroy(gbp_fft_plan plan);
+int gbp_fft_r2c(gbp_fft_plan plan, const float* mesh, void* spectrum,
+                void* workspace, size_t workspace_bytes, gbp_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * Bin edges -> exact integer thresholds (host-only helper, no GPU).
+ * kedges_grid[0..n_edges-1] are float32 bin edges in units of the
+ * fundamental frequency, i.e. k_edges / kF computed in float32 as
+ * src/correlations.py:12,42 does.  Mode (kx,ky,kz) with k2 = kx^2+ky^2+kz^2
+ * falls in bin b (0 <= b < n_edges-1) iff
+ *      thr[b] <= k2 < thr[b+1]               for b < n_edges-2,
+ *      thr[b] <= k2 <= *thr_last_closed      for the last bin,
+ * which is jnp.histogram (searchsorted right, last edge closed) applied to
+ * k = sqrtf((float)k2), bit for bit.  thr has n_edges entries.
+ * *n_reach = number of bins some mode of an n_mesh^3 grid can fall in.
+ * Returns GBP_ERR_INVALID for decreasing or non-finite edges.
+ * ---------------------------------------------------------------------- */
+int gbp_bin_thresholds(const float* kedges_grid, int n_edges, int n_mesh,
+                       int32_t* thr, int32_t* thr_last_closed, int* n_reach);
+
+/* ------------------------------------------------------------------------
+ * Bin plans: thresholds, their lookup table and the per-axis window and
+ * interlacing-phase tables for one (edges, n_mesh), uploaded once to the
+ * current device (the plan owns that memory; gbp_bins_destroy frees it).
+ * kedges_grid is a HOST array, as for gbp_bin_thresholds.
+ * ---------------------------------------------------------------------- */
+typedef struct gbp_bins_s* gbp_bins;
+
+int gbp_bins_create(const float* kedges_grid, int n_edges, int n_mesh,
+                    gbp_bins* bins);
+int gbp_bins_destroy(gbp_bins bins);
+int gbp_bins_info(gbp_bins bins, int* n_bins, int* n_reach,
+                  int32_t* thr_last_closed);
+
+/* ------------------------------------------------------------------------
+ * Power multipoles: fused window deconvolution, interlacing combination,
+ * |delta_k|^2 x L_l(mu) (line of sight = z) and k-shell binning.
+ * Replaces src/correlations.py:20-48 (the body of powspec_vec).
+ *
+ *   spectrum     complex64 [n_grids][n_mesh][n_mesh][n_mesh/2+1].
+ *   n_grids      1, or 2 for an interlaced pair: the modes are combined as
+ *                (F0 + F1 exp(i pi (kx+ky+kz)/n_mesh)) / 2.
+ *   mas_order    window: each axis is divided by sinc(pi k_i/n)^mas_order
+ *                (0 = no deconvolution; src/correlations.py:20-21,32 uses 2).
+ *   ells         GBP_ELL0|GBP_ELL2|GBP_ELL4 [| GBP_KSUM].
+ *   mass         NULL, or device double[n_grids]: the mesh totals.  Then the
+ *                k=0 mode is taken as (F(0) - mass), so a raw density mesh
+ *                gives the spectrum of delta = rho/mean - 1 up to the factor
+ *                that gbp_power_normalize applies.
+ *   sums_out     double[n_bins][3]: sum over modes of |d|^2 W^2 L_l(mu)
+ *                for l = 0,2,4 (zero where not requested).
+ *   nmodes_out   int64[n_bins] mode counts (half-space grid cells, as
+ *                src/correlations.py:48 counts them).
+ *   ksum_out     double[n_bins] sum of |k| in grid units (GBP_KSUM), or NULL.
+ * ---------------------------------------------------------------------- */
+int gbp_power_workspace_size(gbp_bins bins, int n_grids, int ells,
+                             size_t* bytes);
+
+int gbp_power(const void* spectrum, int n_grids, gbp_bins bins, int mas_order,
+              int ells, const double* mass, double* sums_out,
+              long long* nmodes_out, double* ksum_out, void* workspace,
+              size_t workspace_bytes, gbp_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * Normalisation of gbp_power's sums into P_l(k), on the device.
+ * Replaces src/correlations.py:49-54 (and the caller-side shot-noise
+ * subtraction of tests/correlations.py:36,83).
+ *   P_l[b] = (2l+1) * sums[b][l] / nmodes[b] * norm  - shot*(l==0)
+ *   norm   = (box/n^2)^3            when mass == NULL (delta given)
+ *          = box^3 / mass[0]^2      when mass != NULL (raw density mesh)
+ *   shot   = box^3 * sum_w2 / mass[0]^2 when subtract_shot and stats given.
+ *   kmean[b] = ksum[b] / nmodes[b] * 2 pi / box   (when ksum != NULL)
+ * Empty bins give NaN, as in the reference (0/0).
+ * ---------------------------------------------------------------------- */
+int gbp_power_normalize(const double* sums, const long long* nmodes,
+                        const double* ksum, int n_bins, int n_mesh,
+                        double box_size, const double* mass,
+                        const gbp_deposit_stats* stats, int subtract_shot,
+                        double* pk_out, double* kmean_out,
+                        gbp_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBPOWSPEC_H */

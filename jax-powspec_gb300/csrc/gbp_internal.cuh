@@ -1,0 +1,68 @@
+// Internal helpers shared by the gbpowspec CUDA translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gbpowspec.h"
+
+#define GBP_CUDA_TRY(expr)                                   \
+  do {                                                       \
+    cudaError_t e_ = (expr);                                 \
+    if (e_ != cudaSuccess) { gbp::set_last_cuda_error(e_); return GBP_ERR_CUDA; } \
+  } while (0)
+
+#define GBP_LAUNCH_CHECK()                                   \
+  do {                                                       \
+    cudaError_t e_ = cudaGetLastError();                     \
+    if (e_ != cudaSuccess) { gbp::set_last_cuda_error(e_); return GBP_ERR_CUDA; } \
+  } while (0)
+
+namespace gbp {
+
+void set_last_cuda_error(cudaError_t e);
+
+// Bytes rounded up to a multiple of 256 (keeps every workspace slice aligned).
+inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+// Carve consecutive 256-byte-aligned slices out of a caller workspace.
+struct Carver {
+  char* base;
+  size_t used = 0;
+  explicit Carver(void* p) : base(static_cast<char*>(p)) {}
+  template <class T>
+  T* take(size_t count) {
+    T* p = reinterpret_cast<T*>(base ? base + used : nullptr);
+    used += align256(count * sizeof(T));
+    return p;
+  }
+};
+
+__host__ __device__ inline int pmod(int a, int n) {
+  int r = a % n;
+  return r < 0 ? r + n : r;
+}
+
+// Signed wavenumber of FFT index i on an n-point axis, as the reference
+// builds it: ki = i if i <= n/2 else i - n (src/correlations.py:25).
+__host__ __device__ inline int signed_k(int i, int n) { return i > n / 2 ? i - n : i; }
+
+// ---- float-float ("double-single") arithmetic ----------------------------
+// GB300 runs FP64 at a small fraction of its FP32 rate, so wide reductions
+// keep a (hi, lo) pair of floats and combine them with error-free sums
+// (Knuth TwoSum); only the final per-bin totals are converted to double.
+struct ff { float hi, lo; };
+
+__device__ __forceinline__ ff ff_add(ff a, ff b) {
+  float s = __fadd_rn(a.hi, b.hi);
+  float v = __fsub_rn(s, a.hi);
+  float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, v)), __fsub_rn(b.hi, v));
+  e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+  float hi = __fadd_rn(s, e);
+  float lo = __fsub_rn(e, __fsub_rn(hi, s));
+  return {hi, lo};
+}
+
+__device__ __forceinline__ ff ff_add_f(ff a, float b) { return ff_add(a, ff{b, 0.0f}); }
+
+}  // namespace gbp

@@ -1,0 +1,135 @@
+"""P(k) multipoles: drop-ins for jax-powspec's src/correlations.py P(k) path.
+
+``powspec_vec(delta, box_size, k_edges)`` and
+``powspec_vec_fundamental(delta, box_size)`` keep the reference's signatures
+and return tuples ``(k3D, Pk3D, Nmodes3D)`` as float32 CUDA tensors:
+
+* the mesh is FFT'd with cuFFT (R2C), then one fused kernel applies the CIC
+  window correction (1/sinc)^2 per axis (src/correlations.py:20-21,32,39),
+  squares, weights by L_0, L_2, L_4 of mu = kz/k (:36-38,45-47) and bins;
+* binning reproduces jnp.histogram on k = sqrtf(kx^2+ky^2+kz^2) against the
+  float32 edges k_edges / kF (:34,42), so mode counts are bit-identical;
+* P_l = (2l+1) sum / N_modes * (L/N^2)^3 (:49-52), NaN in empty bins;
+* k3D are the arithmetic bin centres (:54).
+
+Per-bin sums are accumulated in FP32 inside a warp and in float-float /
+FP64 beyond, so they are more accurate than the reference's float32
+scatter-add; P agrees with it to float32 rounding.
+"""
+from __future__ import annotations
+
+import functools
+
+import numpy as np
+import torch
+
+from . import _lib, _native
+
+__all__ = ["powspec_vec", "powspec_vec_fundamental", "reference_kedges", "default_kedges"]
+
+_F32 = np.float32
+
+
+def _box_f32(box_size) -> np.float32:
+    if isinstance(box_size, torch.Tensor):
+        box_size = box_size.detach().reshape(()).cpu().item()
+    return _F32(np.asarray(box_size, dtype=np.float32).reshape(()))
+
+
+def reference_kedges(k_edges, box_size):
+    """(k_edges / kF, kF) in float32 with kF = 2 pi / box (src/correlations.py:12,42)."""
+    if isinstance(k_edges, torch.Tensor):
+        k_edges = k_edges.detach().cpu().numpy()
+    kf = _F32(_F32(2.0 * np.pi) / _box_f32(box_size))
+    ke = np.asarray(k_edges, dtype=np.float32).reshape(-1)
+    return (ke / kf).astype(np.float32), kf
+
+
+def default_kedges(n_mesh: int, box_size: float) -> np.ndarray:
+    """k edges from kF to k_Nyquist in steps of kF (h/Mpc), as float32."""
+    kf = 2.0 * np.pi / float(box_size)
+    return np.arange(kf, np.pi * n_mesh / float(box_size), kf).astype(np.float32)
+
+
+def _cubic_mesh(delta) -> torch.Tensor:
+    d = _native.as_cuda_f32(delta, name="delta")
+    if d.ndim != 3 or not (d.shape[0] == d.shape[1] == d.shape[2]):
+        raise ValueError(f"delta must be a cubic 3-D mesh, got shape {tuple(d.shape)}")
+    return d
+
+
+def _binned_power(d: torch.Tensor, kedges_grid: np.ndarray, box: np.float32):
+    N = int(d.shape[0])
+    dev = d.device
+    bins = _native.bins_for(kedges_grid, N, dev)
+    plan = _native.fft_plan(N, 1, dev)
+    spec = torch.empty(N * N * (N // 2 + 1) * 2, dtype=torch.float32, device=dev)
+    plan.execute(d, spec)
+    ps = _native.power(spec, 1, bins, mas_order=2, ells=_lib.ELL0 | _lib.ELL2 | _lib.ELL4)
+    pk, _ = _native.normalize(ps, n_mesh=N, box_size=float(box))
+    return ps, pk
+
+
+def powspec_vec(delta, box_size, k_edges):
+    """Drop-in for src/correlations.py:7-56 (``powspec_vec``)."""
+    d = _cubic_mesh(delta)
+    kedges, kf = reference_kedges(k_edges, box_size)
+    ps, pk = _binned_power(d, kedges, _box_f32(box_size))
+    k3d = ((_F32(0.5) * (kedges[1:] + kedges[:-1])) * kf).astype(np.float32)
+    return (torch.from_numpy(k3d).to(d.device), pk.to(torch.float32), ps.nmodes.to(torch.float32))
+
+
+@functools.lru_cache(maxsize=8)
+def _fundamental_last_k(N: int) -> np.ndarray:
+    """float32 |k| of the LAST mode (C order over the rfft grid) in each slot int32(|k|).
+
+    src/correlations.py:100 sets k3D[int32(k)] = k for every mode with one
+    scatter; the reference's CPU path applies duplicate writes in order, so
+    the surviving value is the last mode's.  This is pure geometry.
+    """
+    h = N // 2
+    kmax = int(np.int32(np.sqrt(np.float32(3 * h * h))))
+    out = np.zeros(kmax + 1, dtype=np.float32)
+    found = np.zeros(kmax + 1, dtype=bool)
+    ki = np.where(np.arange(N) > h, np.arange(N) - N, np.arange(N)).astype(np.int64)
+    kz2 = (ki[: h + 1] ** 2)[None, :]
+    ky2 = (ki ** 2)[:, None]
+    for ix in range(N - 1, -1, -1):
+        k2 = ki[ix] ** 2 + ky2 + kz2                          # [N, h+1], C order = (iy, iz)
+        kk = np.sqrt(k2.astype(np.float32)).ravel()
+        slot = kk.astype(np.int32)
+        todo = ~found[slot]
+        if not todo.any():
+            continue
+        # last occurrence of each slot in this plane
+        rev = slot[::-1]
+        uniq, first_rev = np.unique(rev, return_index=True)
+        last_idx = kk.size - 1 - first_rev
+        new = ~found[uniq]
+        out[uniq[new]] = kk[last_idx[new]]
+        found[uniq[new]] = True
+        if found.all():
+            break
+    return out
+
+
+def powspec_vec_fundamental(delta, box_size):
+    """Drop-in for src/correlations.py:60-117 (``powspec_vec_fundamental``).
+
+    Bins are the integer shells int32(|k|) = 1 .. kmax (slot 0 dropped, :106-109).
+    The returned k3D keeps the reference's formula (:100,110): the |k| of the
+    last mode written to each slot, divided by the slot's mode count, times kF.
+    """
+    d = _cubic_mesh(delta)
+    N = int(d.shape[0])
+    h = N // 2
+    kmax = int(np.int32(np.sqrt(np.float32(3 * h * h))))
+    edges = np.arange(kmax + 2, dtype=np.float32)              # slot i = [i, i+1)
+    box = _box_f32(box_size)
+    # not jitted in the reference: kF is a Python float64, rounded where it meets float32 (:64,:110)
+    kf = _F32(2.0 * np.pi / float(box_size))
+    ps, pk = _binned_power(d, edges, box)
+    nmodes = ps.nmodes.to(torch.float32)
+    lastk = torch.from_numpy(_fundamental_last_k(N)).to(d.device)
+    k3d = (lastk / nmodes) * float(kf)
+    return k3d[1:], pk[1:].to(torch.float32), nmodes[1:]

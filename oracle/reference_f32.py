@@ -1,0 +1,217 @@
+"""TEST ORACLE -- not product code.  Only tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline leg may import this module, and only as the checker or
+as the timed CPU stand-in for the reference.
+
+A numpy restatement, in float32 where the reference computes in float32, of
+jax-powspec's P(k) path (dforero0896/jax-powspec, src/mas.py and
+src/correlations.py).  Each function cites the reference lines it follows.
+
+JAX itself is absent from this environment, so the JAX primitives the
+reference relies on are restated from their published semantics:
+  * ``x.at[idx].add(v)`` (scatter-add): updates applied in order; negative
+    indices count once from the end, indices still outside [0, n) drop the
+    update (jax's default FILL_OR_DROP for scatters).  ``np.add.at`` on a
+    float32 array accumulates sequentially in float32, like XLA:CPU.
+  * ``jnp.histogram(a, bins, weights)``: ``searchsorted(bins, a, 'right')``,
+    values equal to the last edge go to the last bin, then
+    ``zeros(len(bins)).at[idx].add(weights)[1:]``.
+  * ``jnp.int32(x)`` truncates toward zero; ``jnp.sqrt`` of an int32 array is
+    computed in float32 (x64 disabled).
+  * ``jnp.fft.rfftn`` in complex64 (scipy.fft's single-precision pocketfft
+    stands in for ducc).
+The restatement is pinned against fixtures produced by running the
+reference's own source (tests/golden/make_golden.py).
+"""
+from __future__ import annotations
+
+import numpy as np
+import scipy.fft
+
+F32 = np.float32
+
+
+def _f32(v) -> np.float32:
+    return F32(np.asarray(v, dtype=np.float32).reshape(()))
+
+
+def scatter_add(mesh: np.ndarray, idx, vals: np.ndarray) -> None:
+    """In-place ``mesh.at[idx].add(vals)`` with jax's default index rules."""
+    ok = np.ones(vals.shape, dtype=bool)
+    norm = []
+    for a, n in zip(idx, mesh.shape):
+        a = np.asarray(a).astype(np.int64)
+        a = np.where(a < 0, a + n, a)
+        ok &= (a >= 0) & (a < n)
+        norm.append(a)
+    np.add.at(mesh, tuple(a[ok] for a in norm), vals.astype(mesh.dtype)[ok])
+
+
+def _inv_bin_size(box_size, n_bins):
+    bin_size = _f32(box_size) / F32(n_bins)          # src/mas.py:100 (and :17)
+    return F32(F32(1.0) / bin_size)                  # src/mas.py:101 (and :18)
+
+
+def cic_mas_vec(delta, x, y, z, w, n_part, xmin, ymin, zmin, box_size, n_bins, wrap):
+    """src/mas.py:88-153."""
+    inv = _inv_bin_size(box_size, n_bins)
+    pos = [(np.asarray(c, F32) - _f32(o)) * inv for c, o in ((x, xmin), (y, ymin), (z, zmin))]  # :103-105
+    i0 = [p.astype(np.int32) for p in pos]                                  # :107-109 (trunc)
+    dd = [p - i.astype(F32) for p, i in zip(pos, i0)]                       # :111-113
+    ip = [i + 1 for i in i0]                                                 # :115-117
+    n = int(n_bins)
+    if wrap:                                                                  # :119-122
+        ip = [np.mod(i + n, n) for i in ip]
+    else:                                                                     # :123-134
+        new_ip, new_dd = [], []
+        for i, d in zip(ip, dd):
+            i = np.where(i >= n, 0, i)
+            d = np.where(i >= n, F32(0), d)       # tests the already-zeroed index: never true
+            new_ip.append(i)
+            new_dd.append(d.astype(F32))
+        ip, dd = new_ip, new_dd
+    md = [F32(1.0) - d for d in dd]                                          # :138-140
+    w = np.ones_like(pos[0]) if w is None else np.asarray(w, F32)
+    (ix, iy, iz), (ixp, iyp, izp) = i0, ip
+    (dx, dy, dz), (mx, my, mz) = dd, md
+    out = np.array(delta, dtype=F32, copy=True)
+    scatter_add(out, (ix, iy, iz), mx * my * mz * w)                          # :142
+    scatter_add(out, (ixp, iy, iz), dx * my * mz * w)                         # :143
+    scatter_add(out, (ix, iyp, iz), mx * dy * mz * w)                         # :144
+    scatter_add(out, (ix, iy, izp), mx * my * dz * w)                         # :145
+    scatter_add(out, (ixp, iyp, iz), dx * dy * mz * w)                        # :147
+    scatter_add(out, (ixp, iy, izp), dx * my * dz * w)                        # :148
+    scatter_add(out, (ix, iyp, izp), mx * my * dz * w)                        # :149 (sic: mdy)
+    scatter_add(out, (ixp, iyp, izp), dx * dy * dz * w)                       # :151
+    return out
+
+
+def cic_mas(delta, x, y, z, w, n_part, xmin, ymin, zmin, box_size, n_bins, wrap):
+    """src/mas.py:5-87: a lax.scan over particles doing 8 scatter-adds each."""
+    inv = _inv_bin_size(box_size, n_bins)
+    n = int(n_bins)
+    out = np.array(delta, dtype=F32, copy=True)
+    xs, ys, zs = (np.asarray(c, F32) for c in (x, y, z))
+    ws = np.ones_like(xs) if w is None else np.asarray(w, F32)
+    o = (_f32(xmin), _f32(ymin), _f32(zmin))
+    for p in range(xs.size):
+        pos = [(c[p] - oo) * inv for c, oo in zip((xs, ys, zs), o)]          # :44-46
+        i0 = [int(np.int32(q)) for q in pos]                                  # :48-50
+        dd = [F32(q - F32(i)) for q, i in zip(pos, i0)]                       # :52-54
+        md = [F32(F32(1.0) - d) for d in dd]                                  # :56-58 (before the cond)
+        ip = [i + 1 for i in i0]                                              # :60-62
+        if wrap:                                                              # :20-28
+            ip = [i - n if i >= n else i for i in ip]
+        else:                                                                 # :30-38
+            for k in range(3):
+                if ip[k] >= n:
+                    ip[k], dd[k] = 0, F32(0.0)
+        wt = ws[p]
+        (ix, iy, iz), (ixp, iyp, izp) = i0, ip
+        (dx, dy, dz), (mx, my, mz) = dd, md
+        for idx, val in (((ix, iy, iz), mx * my * mz * wt),                   # :69
+                         ((ixp, iy, iz), dx * my * mz * wt),                  # :70
+                         ((ix, iyp, iz), mx * dy * mz * wt),                  # :71
+                         ((ix, iy, izp), mx * my * dz * wt),                  # :72
+                         ((ixp, iyp, iz), dx * dy * mz * wt),                 # :74
+                         ((ixp, iy, izp), dx * my * dz * wt),                 # :75
+                         ((ix, iyp, izp), mx * my * dz * wt),                 # :76 (sic: mdy)
+                         ((ixp, iyp, izp), dx * dy * dz * wt)):               # :78
+            scatter_add(out, tuple(np.array([i]) for i in idx), np.array([val], F32))
+    return out
+
+
+def histogram_f32(a: np.ndarray, edges: np.ndarray, weights: np.ndarray | None):
+    """jnp.histogram with array bins: right-searchsorted, last edge closed, float32 scatter-add."""
+    a = np.asarray(a, F32).ravel()
+    edges = np.asarray(edges, F32)
+    idx = np.searchsorted(edges, a, side="right")
+    idx = np.where(a == edges[-1], edges.size - 1, idx)
+    wts = np.ones_like(a) if weights is None else np.asarray(weights, F32).ravel()
+    counts = np.zeros(edges.size, F32)
+    keep = idx < edges.size                      # the out-of-range index is dropped
+    np.add.at(counts, idx[keep], wts[keep])
+    return counts[1:]
+
+
+def _kgrid(dims: int):
+    middle = dims // 2
+    r = np.arange(dims, dtype=np.int32)
+    ki = np.where(r > middle, r - dims, r).astype(np.int32)                     # src/correlations.py:25
+    kx = np.broadcast_to(ki[:, None, None], (dims, dims, middle + 1))           # :29
+    ky = np.broadcast_to(ki[None, :, None], (dims, dims, middle + 1))           # :30
+    kz = np.broadcast_to(ki[None, None, : middle + 1], (dims, dims, middle + 1))  # :31
+    return kx, ky, kz
+
+
+def _cic_correction(kk: np.ndarray, dims: int) -> np.ndarray:
+    """(1 / jnp.sinc(prefact*k / pi))**2 in float32 (src/correlations.py:15,20-21)."""
+    prefact = F32(np.pi / dims)
+    x = (prefact * kk.astype(F32)) / F32(np.pi)
+    s = np.sinc(x).astype(F32)
+    return (F32(1.0) / s) ** F32(2.0)
+
+
+def _power_core(delta, box_size):
+    dims = delta.shape[0]
+    delta_k = scipy.fft.rfftn(np.asarray(delta, F32), axes=(0, 1, 2)).astype(np.complex64)  # :22
+    kx, ky, kz = _kgrid(dims)
+    corr = _cic_correction(kx, dims) * _cic_correction(ky, dims) * _cic_correction(kz, dims)  # :32
+    k = np.sqrt((kx * kx + ky * ky + kz * kz).astype(F32))                  # :34
+    with np.errstate(invalid="ignore", divide="ignore"):
+        mu = np.where(k == 0, F32(0), kz.astype(F32) / k).astype(F32)       # :36-37
+    mu2 = (mu ** 2).ravel()                                                 # :38
+    delta_k = (delta_k * corr).astype(np.complex64)                         # :39
+    delta2 = (delta_k * delta_k.conj()).real.astype(F32).ravel()            # :40
+    return dims, k, mu2, delta2
+
+
+def powspec_vec(delta, box_size, k_edges):
+    """src/correlations.py:7-56."""
+    dims, k, mu2, delta2 = _power_core(delta, box_size)
+    kF = F32(F32(2.0 * np.pi) / _f32(box_size))                              # :12
+    kedges = (np.asarray(k_edges, F32) / kF).astype(F32)                     # :42
+    kf = k.ravel()
+    mono = histogram_f32(kf, kedges, delta2)                                  # :45
+    quad = histogram_f32(kf, kedges, delta2 * (F32(3.0) * mu2 - F32(1.0)) / F32(2.0))       # :46
+    hexa = histogram_f32(kf, kedges, delta2 * (F32(35.0) * mu2 * mu2 - F32(30.0) * mu2 + F32(3.0)) / F32(8.0))  # :47
+    nmodes = histogram_f32(kf, kedges, None)                                  # :48
+    norm = (_f32(box_size) / F32(dims ** 2)) ** 3
+    with np.errstate(invalid="ignore", divide="ignore"):
+        pk = np.zeros((mono.size, 3), F32)
+        pk[:, 0] = mono / nmodes * norm                                       # :50
+        pk[:, 1] = quad / nmodes * F32(5.0) * norm                            # :51
+        pk[:, 2] = hexa / nmodes * F32(9.0) * norm                            # :52
+    k3d = (F32(0.5) * (kedges[1:] + kedges[:-1])) * kF                        # :54
+    return k3d.astype(F32), pk, nmodes
+
+
+def powspec_vec_fundamental(delta, box_size):
+    """src/correlations.py:60-117 (k3D keeps the last-writer scatter-set of :100).
+
+    This function is not jitted in the reference, so with a Python float box
+    size its constants kF (:64) and (box/dims^2)^3 (:112) are Python float64
+    values, rounded to float32 only where they meet a float32 array.
+    """
+    dims, k, mu2, delta2 = _power_core(delta, box_size)
+    middle = dims // 2
+    kF = F32(2.0 * np.pi / float(box_size))                                   # :64
+    kmax = int(np.int32(np.sqrt(F32(3 * middle * middle))))                   # :69
+    kf = k.ravel()
+    kidx = kf.astype(np.int32)                                                # :87
+    k3d = np.zeros(kmax + 1, F32)
+    k3d[kidx] = kf            # numpy fancy assignment keeps the last duplicate   :100
+    pk = np.zeros((kmax + 1, 3), F32)
+    np.add.at(pk[:, 0], kidx, delta2)                                         # :101
+    np.add.at(pk[:, 1], kidx, delta2 * (F32(3.0) * mu2 - F32(1.0)) / F32(2.0))  # :102
+    np.add.at(pk[:, 2], kidx, delta2 * (F32(35.0) * mu2 * mu2 - F32(30.0) * mu2 + F32(3.0)) / F32(8.0))  # :103
+    nmodes = np.zeros(kmax + 1, F32)
+    np.add.at(nmodes, kidx, F32(1.0))                                         # :104
+    k3d, nmodes, pk = k3d[1:], nmodes[1:], pk[1:]                             # :106-108
+    norm = F32((float(box_size) / dims ** 2) ** 3)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        k3d = k3d / nmodes * kF                                               # :110
+        out = np.zeros_like(pk)
+        out[:, 0] = pk[:, 0] / nmodes * norm                                  # :112
+        out[:, 1] = pk[:, 1] / nmodes * F32(5.0) * norm                       # :113
+        out[:, 2] = pk[:, 2] / nmodes * F32(9.0) * norm                       # :114
+    return k3d.astype(F32), out, nmodes
