@@ -156,7 +156,19 @@ def main():
     ap.add_argument("--steps-ref", type=int, default=2)
     ap.add_argument("--warmup-ref", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--n-mesh", type=int, default=None, help="override the mesh side (profiling cases)")
+    ap.add_argument("--n-particles", type=int, default=None, help="override the particle count")
+    ap.add_argument("--profile-only", action="store_true",
+                    help="warm-up + timed steps only (no stage/e2e/CPU legs): a short command for ncu")
     args = ap.parse_args()
+    if args.n_mesh:
+        CONFIG["n_mesh"] = args.n_mesh
+        CONFIG["field_grid"] = min(256, args.n_mesh)
+    if args.n_particles:
+        CONFIG["n_particles"] = args.n_particles
+    if args.n_mesh or args.n_particles:
+        CONFIG["workload"] = (f"lognormal+RSD {CONFIG['n_mesh']}^3 TSC+interlaced P_0,2,4 "
+                              f"({CONFIG['n_particles']:,} particles, L={CONFIG['box']:g}) [override]")
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
@@ -207,6 +219,13 @@ def main():
     barrier()
     t_dev = e0.elapsed_time(e1) / 1e3
     clk = clocks.stop()
+    if args.profile_only:
+        if rank == 0:
+            print(json.dumps({"profile_only": True, "ms_per_step": t_dev / args.steps * 1e3,
+                              "config": _cfg_json()}), flush=True)
+        if ws > 1:
+            dist.destroy_process_group()
+        return
 
     # ---- stage breakdown (instrumented loop, events between the stages)
     N, G = cfg.n_mesh, cfg.grids

@@ -117,6 +117,31 @@ extern "C" int gbp_bins_create(const float* e, int ne, int N, gbp_bins* out) {
     while (r <= B->nbe && h_thr[r] <= key) ++r;
     h_lut[j] = r;
   }
+  // Mode counts and sum of |k| per bin depend only on the grid: count the
+  // half-space cells per k^2 value once (pairs |kx|,|ky| with multiplicity),
+  // then fold them into bins in increasing k^2 order (deterministic).
+  std::vector<long long> per_k2((size_t)K + 1, 0);
+  for (int ax = 0; ax <= h; ++ax) {
+    const long long mx = (ax == 0 || (N % 2 == 0 && ax == h)) ? 1 : 2;
+    for (int ay = 0; ay <= h; ++ay) {
+      const long long my = (ay == 0 || (N % 2 == 0 && ay == h)) ? 1 : 2;
+      const long long kp2 = (long long)ax * ax + (long long)ay * ay;
+      for (int kz = 0; kz <= h; ++kz) per_k2[kp2 + (long long)kz * kz] += mx * my;
+    }
+  }
+  std::vector<long long> h_nmodes((size_t)B->nb, 0);
+  std::vector<double> h_ksum((size_t)B->nb, 0.0);
+  {
+    int r = 0;                                   // #thresholds <= k2, non-decreasing in k2
+    for (long long k2 = 0; k2 <= K && k2 <= last; ++k2) {
+      while (r < ne && thr[r] <= k2) ++r;
+      const long long c = per_k2[k2];
+      if (!c || r == 0) continue;
+      const int b = (r < B->nb ? r : B->nb) - 1;
+      h_nmodes[b] += c;
+      h_ksum[b] += (double)c * sqrt((double)k2);
+    }
+  }
   std::vector<float> h_is2(h + 1);
   std::vector<float2> h_eph(h + 1);
   for (int k = 0; k <= h; ++k) {
@@ -129,7 +154,9 @@ extern "C" int gbp_bins_create(const float* e, int ne, int N, gbp_bins* out) {
   const size_t o_lut = o_thr + align256(h_thr.size() * 4);
   const size_t o_is2 = o_lut + align256(h_lut.size() * 4);
   const size_t o_eph = o_is2 + align256(h_is2.size() * 4);
-  const size_t total = o_eph + align256(h_eph.size() * 8);
+  const size_t o_nm = o_eph + align256(h_eph.size() * 8);
+  const size_t o_ks = o_nm + align256(h_nmodes.size() * 8);
+  const size_t total = o_ks + align256(h_ksum.size() * 8);
   cudaGetDevice(&B->device);
   char* blk = nullptr;
   if (cudaMalloc(&blk, total) != cudaSuccess) {
@@ -141,7 +168,11 @@ extern "C" int gbp_bins_create(const float* e, int ne, int N, gbp_bins* out) {
   B->d_lut = reinterpret_cast<int*>(blk + o_lut);
   B->d_inv_sinc2 = reinterpret_cast<float*>(blk + o_is2);
   B->d_eph = reinterpret_cast<float2*>(blk + o_eph);
+  B->d_nmodes = reinterpret_cast<long long*>(blk + o_nm);
+  B->d_ksum = reinterpret_cast<double*>(blk + o_ks);
   cudaError_t ce = cudaSuccess;
+  if (ce == cudaSuccess) ce = cudaMemcpy(B->d_nmodes, h_nmodes.data(), h_nmodes.size() * 8, cudaMemcpyHostToDevice);
+  if (ce == cudaSuccess) ce = cudaMemcpy(B->d_ksum, h_ksum.data(), h_ksum.size() * 8, cudaMemcpyHostToDevice);
   if (ce == cudaSuccess) ce = cudaMemcpy(B->d_thr, h_thr.data(), h_thr.size() * 4, cudaMemcpyHostToDevice);
   if (ce == cudaSuccess) ce = cudaMemcpy(B->d_lut, h_lut.data(), h_lut.size() * 4, cudaMemcpyHostToDevice);
   if (ce == cudaSuccess) ce = cudaMemcpy(B->d_inv_sinc2, h_is2.data(), h_is2.size() * 4, cudaMemcpyHostToDevice);

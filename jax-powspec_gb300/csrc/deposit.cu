@@ -2,22 +2,24 @@
 // the two reference-compatible CIC variants of src/mas.py).
 //
 // Pipeline (all on one stream, deterministic):
-//   1. count_kernel    every particle adds 1 to each 16^3 mesh tile that its
-//                      stencil touches (integer atomics: order-free), and
-//                      reduces max|w|, sum w, sum w^2 per block.
+//   1. count_kernel    every particle adds 1 to each mesh tile (16^3 cells)
+//                      that its stencil touches (integer atomics: the counts
+//                      do not depend on order), and reduces max|w|, sum w and
+//                      sum w^2 per block.
 //   2. cub scan        exclusive prefix sum of the tile counts -> cursors.
-//   3. scatter_kernel  every particle appends its grid coordinate + weight to
-//                      each touched tile's bucket (a one-digit radix sort of
-//                      the particles by tile, with replication at tile faces).
+//   3. scatter_kernel  every particle appends (u_x, u_y, u_z, w) to each
+//                      touched tile's bucket: a one-digit radix sort of the
+//                      particles by tile, replicated across tile faces.
 //   4. deposit_kernel  one CTA per tile accumulates its bucket in shared
 //                      memory in int64 fixed point (scale 2^s fixed by n and
-//                      max|w|), then writes the tile of the mesh exactly once.
+//                      max|w|), then writes its cells of the mesh exactly once.
 //   5. stats_kernel    folds the per-block partial sums in a fixed order.
 //
-// Fixed-point accumulation makes the sum independent of particle order and
-// scheduling, so the mesh is bitwise reproducible; no float atomics are used
-// anywhere.  Every mesh cell is written once (zeros included), so no separate
-// clearing pass is needed.
+// Integer accumulation makes each cell's sum independent of particle order
+// and scheduling, so the mesh is bitwise reproducible; no float atomics are
+// used.  Every cell is written once (zeros included): no clearing pass.
+// The scheme (MAS order, number of grids, reference-compat variant) is a
+// template parameter so every stencil lives in registers.
 #include <cub/device/device_scan.cuh>
 
 #include "gbp_internal.cuh"
@@ -40,142 +42,162 @@ struct DepGeom {
   long long n;
   float ox, oy, oz, inv_cell;
   int N;
-  int mas;          // 1..4 (compat modes: 2)
-  int G;            // grids (1, or 2 when interlaced)
-  int compat;       // GBP_COMPAT_*
-  int wrap;
+  int wrap;         // compat modes only
   int tdim;         // tile edge actually used (min(TILE, N))
+  int tshift;       // log2(tdim) when tdim is a power of two, else -1
   int nt;           // tiles per axis
+  int vec_ok;       // mesh pointers are 16-byte aligned (float4 tile stores allowed)
 };
 
-// Stencil of one particle along one axis: nodes first .. first+R-1
-// (unreduced; taken mod N when used), their weights, and which nodes are
-// valid scatter indices (only the compat modes ever drop nodes).
+// Node index reduced into [0, N).  Stencil nodes lie within a few cells of
+// [0, N); tiny meshes fall back to the general modulo.
+__device__ __forceinline__ int wrapn(int n, int N) {
+  if (N < 8) return pmod(n, N);
+  return n < 0 ? n + N : (n >= N ? n - N : n);
+}
+
+__device__ __forceinline__ int tile_of(const DepGeom& g, int node) {
+  return g.tshift >= 0 ? (node >> g.tshift) : node / g.tdim;
+}
+
+template <int MAS, int CM>
+struct Scheme {
+  static constexpr int R = CM ? 2 : MAS;    // nodes per axis
+};
+
+// One axis of one particle: nodes first .. first+R-1 (not yet wrapped), their
+// weights, and a mask of nodes that are valid scatter indices (only the
+// reference-compat variants ever drop nodes).
+template <int R>
 struct Axis {
   int first;
   unsigned vmask;
-  float w[4];
+  float w[R];
 };
 
-// B-spline weights of order `mas` on nodes at integer grid coordinates
-// (the reference's node convention: node i sits at xmin + i*H).
-// `half` = 1 shifts the particle by +half a cell (second interlaced grid).
-__device__ __forceinline__ void axis_bspline(float u, int mas, int half, Axis& a) {
-  float fu = floorf(u);
+// B-spline of order MAS with nodes at integer grid coordinates (the
+// reference's node convention: node i sits at xmin + i*H).  `half` shifts
+// the particle by +half a cell (the second, interlaced grid).
+template <int MAS>
+__device__ __forceinline__ void axis_bspline(float u, int N, int half, Axis<MAS>& a) {
+  const float fu = floorf(u);
   float d = __fsub_rn(u, fu);                 // exact, in [0, 1)
-  int i = __float2int_rz(fu);
+  int i = pmod(__float2int_rz(fu), N);
   if (half) {
     d = __fadd_rn(d, 0.5f);
     if (d >= 1.0f) { d = __fsub_rn(d, 1.0f); i += 1; }
   }
-  a.vmask = 0xFu;
-  a.w[1] = a.w[2] = a.w[3] = 0.0f;
-  switch (mas) {
-    case GBP_NGP:
-      a.first = i + (d >= 0.5f ? 1 : 0);
-      a.w[0] = 1.0f;
-      break;
-    case GBP_CIC:
-      a.first = i;
-      a.w[0] = __fsub_rn(1.0f, d);
-      a.w[1] = d;
-      break;
-    case GBP_TSC: {
-      int up = d >= 0.5f ? 1 : 0;               // nearest node is i+up
-      float s = up ? __fsub_rn(d, 1.0f) : d;    // offset from it, [-0.5, 0.5)
-      a.first = i + up - 1;
-      float l = 0.5f - s, r = 0.5f + s;
-      a.w[0] = 0.5f * l * l;
-      a.w[1] = 0.75f - s * s;
-      a.w[2] = 0.5f * r * r;
-    } break;
-    default: {                                  // PCS (cubic B-spline)
-      float t = d, m = 1.0f - d;
-      const float c6 = 1.0f / 6.0f;
-      a.first = i - 1;
-      a.w[0] = m * m * m * c6;
-      a.w[1] = (4.0f - 6.0f * t * t + 3.0f * t * t * t) * c6;
-      a.w[2] = (4.0f - 6.0f * m * m + 3.0f * m * m * m) * c6;
-      a.w[3] = t * t * t * c6;
-    } break;
+  a.vmask = (1u << MAS) - 1u;
+  if constexpr (MAS == GBP_NGP) {
+    a.first = i + (d >= 0.5f ? 1 : 0);
+    a.w[0] = 1.0f;
+  } else if constexpr (MAS == GBP_CIC) {
+    a.first = i;
+    a.w[0] = __fsub_rn(1.0f, d);
+    a.w[1] = d;
+  } else if constexpr (MAS == GBP_TSC) {
+    const int up = d >= 0.5f ? 1 : 0;           // nearest node is i+up
+    const float s = up ? __fsub_rn(d, 1.0f) : d;  // offset from it, [-0.5, 0.5)
+    a.first = i + up - 1;
+    const float l = 0.5f - s, r = 0.5f + s;
+    a.w[0] = 0.5f * l * l;
+    a.w[1] = 0.75f - s * s;
+    a.w[2] = 0.5f * r * r;
+  } else {                                      // PCS (cubic B-spline)
+    const float t = d, m = 1.0f - d;
+    const float c6 = 1.0f / 6.0f;
+    a.first = i - 1;
+    a.w[0] = m * m * m * c6;
+    a.w[1] = (4.0f - 6.0f * t * t + 3.0f * t * t * t) * c6;
+    a.w[2] = (4.0f - 6.0f * m * m + 3.0f * m * m * m) * c6;
+    a.w[3] = t * t * t * c6;
   }
 }
 
 // The reference CIC along one axis, bit for bit.
-//   GBP_COMPAT_VEC  follows src/mas.py:103-140 (cic_mas_vec): truncating
+//   CM == GBP_COMPAT_VEC follows src/mas.py:103-140 (cic_mas_vec): truncating
 //     int32 cast (:107), fraction (:111), wrap = floor-mod of ix+1 (:121);
 //     no-wrap zeroes ixp but tests the zeroed value, so the fraction is kept
 //     (:125-126).
-//   GBP_COMPAT_SCAN follows src/mas.py:44-67 (cic_mas): mdx is computed
+//   CM == GBP_COMPAT_SCAN follows src/mas.py:44-67 (cic_mas): mdx is computed
 //     before the wrap branch (:56); wrap subtracts n once (:24); no-wrap sets
 //     both ixp and the fraction to zero (:34).
 // Then the scatter's index rule: -N <= idx < 0 maps to idx+N, anything else
-// out of [0, N) is dropped (jax .at[].add default mode).
-__device__ __forceinline__ void axis_compat(float u, int N, int compat, int wrap, Axis& a) {
-  int ix = __float2int_rz(u);
-  float d = __fsub_rn(u, __int2float_rn(ix));
-  float m = __fsub_rn(1.0f, d);
+// outside [0, N) drops the update (jax .at[].add default mode).
+template <int CM>
+__device__ __forceinline__ void axis_compat(float u, int N, int wrap, Axis<2>& a) {
+  const int ix = __float2int_rz(u);
+  const float d = __fsub_rn(u, __int2float_rn(ix));
+  const float m = __fsub_rn(1.0f, d);
   int ixp = ix + 1;
   float dh = d;
-  if (compat == GBP_COMPAT_VEC) {
+  if (CM == GBP_COMPAT_VEC) {
     if (wrap) ixp = pmod(ixp + N, N);
     else if (ixp >= N) ixp = 0;
   } else {
     if (wrap) { if (ixp >= N) ixp -= N; }
     else if (ixp >= N) { ixp = 0; dh = 0.0f; }
   }
-  bool lo_ok = ix >= -N && ix < N;
-  bool hi_ok = ixp >= -N && ixp < N;
-  int lo = ix < 0 ? ix + N : ix;
-  int hi = ixp < 0 ? ixp + N : ixp;
+  const bool lo_ok = ix >= -N && ix < N;
+  const bool hi_ok = ixp >= -N && ixp < N;
+  const int lo = ix < 0 ? ix + N : ix;
+  const int hi = ixp < 0 ? ixp + N : ixp;
   // When both are valid, hi == lo + 1 (mod N) in every branch above.
   a.first = lo_ok ? lo : hi - 1;
   a.vmask = (lo_ok ? 1u : 0u) | (hi_ok ? 2u : 0u);
   a.w[0] = m;
   a.w[1] = dh;
-  a.w[2] = a.w[3] = 0.0f;
 }
 
-__device__ __forceinline__ int stencil_width(const DepGeom& g) {
-  return g.compat ? 2 : g.mas;
+template <int MAS, int CM>
+__device__ __forceinline__ void make_axis(const DepGeom& g, float u, int grid, Axis<Scheme<MAS, CM>::R>& a) {
+  if constexpr (CM != 0) axis_compat<CM>(u, g.N, g.wrap, a);
+  else axis_bspline<MAS>(u, g.N, grid, a);
 }
 
-// Grid coordinate of a particle along the three axes; false if it must be
-// dropped (non-finite, or so far outside the box that int32 cells overflow).
+// Grid coordinate of a particle; false if it must be dropped (non-finite, or
+// so far outside the box that int32 cells would overflow).
 __device__ __forceinline__ bool grid_coords(const DepGeom& g, long long i, float u[3], float& w) {
   u[0] = __fmul_rn(__fsub_rn(g.x[i], g.ox), g.inv_cell);
   u[1] = __fmul_rn(__fsub_rn(g.y[i], g.oy), g.inv_cell);
   u[2] = __fmul_rn(__fsub_rn(g.z[i], g.oz), g.inv_cell);
   w = g.w ? g.w[i] : 1.0f;
-  bool ok = true;
-#pragma unroll
-  for (int a = 0; a < 3; ++a) ok = ok && (fabsf(u[a]) < MAX_ABS_U);  // false for NaN
-  return ok;
+  return fabsf(u[0]) < MAX_ABS_U && fabsf(u[1]) < MAX_ABS_U && fabsf(u[2]) < MAX_ABS_U;  // false for NaN
 }
 
-__device__ __forceinline__ void make_axis(const DepGeom& g, float u, int grid, Axis& a) {
-  if (g.compat) axis_compat(u, g.N, g.compat, g.wrap, a);
-  else axis_bspline(u, g.mas, grid, a);
-}
-
-// Distinct tiles touched along one axis by the valid nodes of all grids.
-// Returns the number of tiles (0 = the particle deposits nothing).
-__device__ __forceinline__ int axis_tiles(const DepGeom& g, float u, int tl[5]) {
-  const int R = stencil_width(g);
-  int ntl = 0;
-  for (int grid = 0; grid < g.G; ++grid) {
-    Axis a;
-    make_axis(g, u, grid, a);
-    for (int r = 0; r < R; ++r) {
-      if (!((a.vmask >> r) & 1u)) continue;
-      int t = pmod(a.first + r, g.N) / g.tdim;
-      bool seen = false;
-      for (int k = 0; k < ntl; ++k) seen = seen || (tl[k] == t);
-      if (!seen && ntl < 5) tl[ntl++] = t;
-    }
+// Distinct tiles touched along one axis by the valid nodes of all grids
+// (at most 3 because a stencil spans at most 5 nodes and tiles are wider).
+template <int MAS, int G, int CM>
+__device__ __forceinline__ int axis_tiles(const DepGeom& g, float u, int& t0, int& t1, int& t2) {
+  constexpr int R = Scheme<MAS, CM>::R;
+  constexpr int W = R + (G - 1);
+  Axis<R> a;
+  make_axis<MAS, CM>(g, u, 0, a);
+  int lo = a.first, hi = a.first + R - 1;
+  if constexpr (CM != 0) {
+    if (a.vmask == 0u) return 0;
+    if (!(a.vmask & 1u)) lo += 1;
+    if (!(a.vmask & 2u)) hi -= 1;
   }
-  return ntl;
+  if constexpr (G == 2) {
+    Axis<R> b;
+    make_axis<MAS, CM>(g, u, 1, b);
+    hi = b.first + R - 1;                        // b.first is a.first or a.first + 1
+  }
+  int nt = 0;
+  t0 = t1 = t2 = -1;
+#pragma unroll
+  for (int k = 0; k < W; ++k) {
+    if (lo + k > hi) break;
+    const int t = tile_of(g, wrapn(lo + k, g.N));
+    if (t == t0 || t == t1 || t == t2) continue;
+    if (nt == 0) t0 = t; else if (nt == 1) t1 = t; else t2 = t;
+    ++nt;
+  }
+  return nt;
 }
+
+__device__ __forceinline__ int pick3(int k, int a, int b, int c) { return k == 0 ? a : (k == 1 ? b : c); }
 
 __device__ __forceinline__ float warp_max(float v) {
   for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
@@ -199,32 +221,34 @@ struct DepCounters {           // zeroed by one memset per call
 };
 
 // Pass 1: tile occupancy counts + weight statistics.
+template <int MAS, int G, int CM>
 __global__ void __launch_bounds__(CNT_THREADS)
-count_kernel(DepGeom g, unsigned* counts, DepCounters* ctr, float4* block_stats) {
+count_kernel(DepGeom g, unsigned* __restrict__ counts, DepCounters* ctr, float4* block_stats) {
   float maxw = 0.0f;
   ff sw{0.f, 0.f}, sw2{0.f, 0.f};
   unsigned kept = 0, bad = 0;
   const long long base = (long long)blockIdx.x * CNT_THREADS * CNT_ITEMS + threadIdx.x;
+#pragma unroll 2
   for (int k = 0; k < CNT_ITEMS; ++k) {
-    long long i = base + (long long)k * CNT_THREADS;
+    const long long i = base + (long long)k * CNT_THREADS;
     if (i >= g.n) break;
     float u[3], w;
     if (!grid_coords(g, i, u, w)) { ++bad; continue; }
-    int tx[5], ty[5], tz[5];
-    int nx = axis_tiles(g, u[0], tx);
-    int ny = axis_tiles(g, u[1], ty);
-    int nz = axis_tiles(g, u[2], tz);
+    int x0, x1, x2, y0, y1, y2, z0, z1, z2;
+    const int nx = axis_tiles<MAS, G, CM>(g, u[0], x0, x1, x2);
+    const int ny = axis_tiles<MAS, G, CM>(g, u[1], y0, y1, y2);
+    const int nz = axis_tiles<MAS, G, CM>(g, u[2], z0, z1, z2);
     if (nx * ny * nz == 0) continue;
     ++kept;
     for (int a = 0; a < nx; ++a)
       for (int b = 0; b < ny; ++b)
         for (int c = 0; c < nz; ++c)
-          atomicAdd(&counts[(tx[a] * g.nt + ty[b]) * g.nt + tz[c]], 1u);
+          atomicAdd(&counts[(pick3(a, x0, x1, x2) * g.nt + pick3(b, y0, y1, y2)) * g.nt + pick3(c, z0, z1, z2)], 1u);
     maxw = fmaxf(maxw, fabsf(w));
     sw = ff_add_f(sw, w);
     sw2 = ff_add_f(sw2, __fmul_rn(w, w));
   }
-  // block reductions (fixed order -> deterministic partials)
+  // block reductions in a fixed order -> deterministic partials
   __shared__ float s_max[CNT_THREADS / 32];
   __shared__ ff s_sw[CNT_THREADS / 32], s_sw2[CNT_THREADS / 32];
   __shared__ unsigned s_kept, s_bad;
@@ -233,7 +257,7 @@ count_kernel(DepGeom g, unsigned* counts, DepCounters* ctr, float4* block_stats)
   maxw = warp_max(maxw);
   sw = warp_ff_sum(sw);
   sw2 = warp_ff_sum(sw2);
-  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   if (lane == 0) { s_max[wid] = maxw; s_sw[wid] = sw; s_sw2[wid] = sw2; }
   if (kept) atomicAdd(&s_kept, kept);
   if (bad) atomicAdd(&s_bad, bad);
@@ -254,92 +278,105 @@ count_kernel(DepGeom g, unsigned* counts, DepCounters* ctr, float4* block_stats)
 }
 
 // Pass 3: append (u_x, u_y, u_z, w) to every touched tile's bucket.
+template <int MAS, int G, int CM>
 __global__ void __launch_bounds__(CNT_THREADS)
-scatter_kernel(DepGeom g, unsigned* cursors, float4* entries) {
+scatter_kernel(DepGeom g, unsigned* __restrict__ cursors, float4* __restrict__ entries) {
   const long long base = (long long)blockIdx.x * CNT_THREADS * CNT_ITEMS + threadIdx.x;
+#pragma unroll 2
   for (int k = 0; k < CNT_ITEMS; ++k) {
-    long long i = base + (long long)k * CNT_THREADS;
+    const long long i = base + (long long)k * CNT_THREADS;
     if (i >= g.n) break;
     float u[3], w;
     if (!grid_coords(g, i, u, w)) continue;
-    int tx[5], ty[5], tz[5];
-    int nx = axis_tiles(g, u[0], tx);
-    int ny = axis_tiles(g, u[1], ty);
-    int nz = axis_tiles(g, u[2], tz);
+    int x0, x1, x2, y0, y1, y2, z0, z1, z2;
+    const int nx = axis_tiles<MAS, G, CM>(g, u[0], x0, x1, x2);
+    const int ny = axis_tiles<MAS, G, CM>(g, u[1], y0, y1, y2);
+    const int nz = axis_tiles<MAS, G, CM>(g, u[2], z0, z1, z2);
     if (nx * ny * nz == 0) continue;
-    float4 e = make_float4(u[0], u[1], u[2], w);
+    const float4 e = make_float4(u[0], u[1], u[2], w);
     for (int a = 0; a < nx; ++a)
       for (int b = 0; b < ny; ++b)
         for (int c = 0; c < nz; ++c) {
-          unsigned slot = atomicAdd(&cursors[(tx[a] * g.nt + ty[b]) * g.nt + tz[c]], 1u);
-          entries[slot] = e;
+          const int t = (pick3(a, x0, x1, x2) * g.nt + pick3(b, y0, y1, y2)) * g.nt + pick3(c, z0, z1, z2);
+          entries[atomicAdd(&cursors[t], 1u)] = e;
         }
   }
 }
 
 // Fixed-point exponent: every partial sum stays below 2^61 in magnitude.
 __device__ __forceinline__ int fixed_scale_exp(long long n, unsigned maxw_bits, int compat) {
-  double bound = (double)n * (double)__uint_as_float(maxw_bits) * (compat ? 27.0 : 1.0);
+  const double bound = (double)n * (double)__uint_as_float(maxw_bits) * (compat ? 27.0 : 1.0);
   if (!(bound > 0.0) || !isfinite(bound)) return 0;
-  int e = ilogb(bound) + 1;                     // bound < 2^e
-  int s = 61 - e;
+  const int e = ilogb(bound) + 1;               // bound < 2^e
+  const int s = 61 - e;
   return s < -120 ? -120 : (s > 120 ? 120 : s);
 }
 
+// Local (in-tile) coordinate of stencil node r of an axis, or -1.
+template <int R>
+__device__ __forceinline__ void local_nodes(const Axis<R>& a, int N, int t0, int ext, int (&l)[R]) {
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int c = wrapn(a.first + r, N) - t0;
+    l[r] = (((a.vmask >> r) & 1u) && c >= 0 && c < ext) ? c : -1;
+  }
+}
+
 // Pass 4: one CTA per tile.
-template <int G>
+template <int MAS, int G, int CM>
 __global__ void __launch_bounds__(DEP_THREADS)
 deposit_kernel(DepGeom g, const float4* __restrict__ entries, const unsigned* __restrict__ counts,
-               const unsigned* __restrict__ cursors, DepCounters* ctr,
-               const float* __restrict__ mesh_in, float* __restrict__ mesh_out) {
-  extern __shared__ long long acc[];            // [G][TILE3]
+               const unsigned* __restrict__ cursors, DepCounters* ctr, const float* __restrict__ mesh_in,
+               float* __restrict__ mesh_out) {
+  constexpr int R = Scheme<MAS, CM>::R;
+  extern __shared__ __align__(16) long long acc[];   // [G][TILE3]
   const int t = blockIdx.x;
   const int tz = t % g.nt, ty = (t / g.nt) % g.nt, tx = t / (g.nt * g.nt);
   const int x0 = tx * g.tdim, y0 = ty * g.tdim, z0 = tz * g.tdim;
   const int ex = min(g.tdim, g.N - x0), ey = min(g.tdim, g.N - y0), ez = min(g.tdim, g.N - z0);
 
-  for (int k = threadIdx.x; k < G * TILE3; k += DEP_THREADS) acc[k] = 0;
-  const int s = fixed_scale_exp(g.n, ctr->maxw_bits, g.compat);
+  {
+    longlong2* a2 = reinterpret_cast<longlong2*>(acc);
+    for (int k = threadIdx.x; k < G * TILE3 / 2; k += DEP_THREADS) a2[k] = make_longlong2(0, 0);
+  }
+  const int s = fixed_scale_exp(g.n, ctr->maxw_bits, CM);
   const float sc = ldexpf(1.0f, s);
   const float inv_sc = ldexpf(1.0f, -s);
   __syncthreads();
 
   const unsigned end = cursors[t];
   const unsigned beg = end - counts[t];
-  const int R = stencil_width(g);
   for (unsigned i = beg + threadIdx.x; i < end; i += DEP_THREADS) {
     const float4 e = entries[i];
 #pragma unroll
     for (int grid = 0; grid < G; ++grid) {
-      Axis ax, ay, az;
-      make_axis(g, e.x, grid, ax);
-      make_axis(g, e.y, grid, ay);
-      make_axis(g, e.z, grid, az);
-      int lx[4], ly[4], lz[4];
+      Axis<R> ax, ay, az;
+      make_axis<MAS, CM>(g, e.x, grid, ax);
+      make_axis<MAS, CM>(g, e.y, grid, ay);
+      make_axis<MAS, CM>(g, e.z, grid, az);
+      int lx[R], ly[R], lz[R];
+      local_nodes<R>(ax, g.N, x0, ex, lx);
+      local_nodes<R>(ay, g.N, y0, ey, ly);
+      local_nodes<R>(az, g.N, z0, ez, lz);
+      unsigned long long* a = reinterpret_cast<unsigned long long*>(acc + grid * TILE3);
 #pragma unroll
-      for (int r = 0; r < 4; ++r) {
-        int l;
-        l = pmod(ax.first + r, g.N) - x0;
-        lx[r] = (r < R && ((ax.vmask >> r) & 1u) && l >= 0 && l < ex) ? l : -1;
-        l = pmod(ay.first + r, g.N) - y0;
-        ly[r] = (r < R && ((ay.vmask >> r) & 1u) && l >= 0 && l < ey) ? l : -1;
-        l = pmod(az.first + r, g.N) - z0;
-        lz[r] = (r < R && ((az.vmask >> r) & 1u) && l >= 0 && l < ez) ? l : -1;
-      }
-      long long* a = acc + grid * TILE3;
       for (int rx = 0; rx < R; ++rx) {
         if (lx[rx] < 0) continue;
+#pragma unroll
         for (int ry = 0; ry < R; ++ry) {
           if (ly[ry] < 0) continue;
+          // src/mas.py:149 (and :76) weights corner (ix, iyp, izp) with
+          // mdx*mdy*ddz; the compat variants keep that (ryw below).
+          const float wxy = __fmul_rn(ax.w[rx], ay.w[ry]);
+          const float wxy_bug = __fmul_rn(ax.w[rx], ay.w[0]);
+          const int row = (lx[rx] * TILE + ly[ry]) * TILE;
+#pragma unroll
           for (int rz = 0; rz < R; ++rz) {
             if (lz[rz] < 0) continue;
-            // src/mas.py:149 (and :76) weights corner (ix, iyp, izp) with
-            // mdx*mdy*ddz; the compat modes keep that.
-            const int ryw = (g.compat && rx == 0 && ry == 1 && rz == 1) ? 0 : ry;
-            float c = __fmul_rn(__fmul_rn(__fmul_rn(ax.w[rx], ay.w[ryw]), az.w[rz]), e.w);
-            long long q = __float2ll_rn(__fmul_rn(c, sc));
-            atomicAdd(reinterpret_cast<unsigned long long*>(&a[(lx[rx] * TILE + ly[ry]) * TILE + lz[rz]]),
-                      static_cast<unsigned long long>(q));
+            const bool bug = CM != 0 && rx == 0 && ry == 1 && rz == 1;
+            const float c = __fmul_rn(__fmul_rn(bug ? wxy_bug : wxy, az.w[rz]), e.w);
+            const long long q = __float2ll_rn(__fmul_rn(c, sc));
+            atomicAdd(&a[row + lz[rz]], static_cast<unsigned long long>(q));
           }
         }
       }
@@ -350,19 +387,38 @@ deposit_kernel(DepGeom g, const float4* __restrict__ entries, const unsigned* __
   // Write the tile once; sum it exactly for the mean density.
   const long long N = g.N;
   const long long M = N * N * N;
+  const bool vec4 = g.vec_ok && (ez == TILE) && ((g.N & 3) == 0);
 #pragma unroll
   for (int grid = 0; grid < G; ++grid) {
     const long long* a = acc + grid * TILE3;
     long long part = 0;
-    for (int k = threadIdx.x; k < TILE3; k += DEP_THREADS) {
-      const int lz = k % TILE, ly = (k / TILE) % TILE, lx = k / (TILE * TILE);
-      if (lx >= ex || ly >= ey || lz >= ez) continue;
-      const long long q = a[k];
-      part += q;
-      const long long gi = grid * M + ((x0 + lx) * N + (y0 + ly)) * N + (z0 + lz);
-      float v = __fmul_rn(__ll2float_rn(q), inv_sc);
-      if (mesh_in) v = __fadd_rn(mesh_in[gi], v);
-      mesh_out[gi] = v;
+    if (vec4) {
+      for (int k = threadIdx.x; k < TILE3 / 4; k += DEP_THREADS) {
+        const int lz = (k % (TILE / 4)) * 4, ly = (k / (TILE / 4)) % TILE, lx = k / (TILE * TILE / 4);
+        if (lx >= ex || ly >= ey) continue;
+        const longlong2 q01 = reinterpret_cast<const longlong2*>(a)[(lx * TILE + ly) * (TILE / 2) + lz / 2];
+        const longlong2 q23 = reinterpret_cast<const longlong2*>(a)[(lx * TILE + ly) * (TILE / 2) + lz / 2 + 1];
+        part += q01.x + q01.y + q23.x + q23.y;
+        float4 v = make_float4(__fmul_rn(__ll2float_rn(q01.x), inv_sc), __fmul_rn(__ll2float_rn(q01.y), inv_sc),
+                               __fmul_rn(__ll2float_rn(q23.x), inv_sc), __fmul_rn(__ll2float_rn(q23.y), inv_sc));
+        const long long gi = grid * M + ((x0 + lx) * N + (y0 + ly)) * N + (z0 + lz);
+        if (mesh_in) {
+          const float4 b = *reinterpret_cast<const float4*>(mesh_in + gi);
+          v = make_float4(__fadd_rn(b.x, v.x), __fadd_rn(b.y, v.y), __fadd_rn(b.z, v.z), __fadd_rn(b.w, v.w));
+        }
+        *reinterpret_cast<float4*>(mesh_out + gi) = v;
+      }
+    } else {
+      for (int k = threadIdx.x; k < TILE3; k += DEP_THREADS) {
+        const int lz = k % TILE, ly = (k / TILE) % TILE, lx = k / (TILE * TILE);
+        if (lx >= ex || ly >= ey || lz >= ez) continue;
+        const long long q = a[k];
+        part += q;
+        const long long gi = grid * M + ((x0 + lx) * N + (y0 + ly)) * N + (z0 + lz);
+        float v = __fmul_rn(__ll2float_rn(q), inv_sc);
+        if (mesh_in) v = __fadd_rn(mesh_in[gi], v);
+        mesh_out[gi] = v;
+      }
     }
     for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
     if ((threadIdx.x & 31) == 0 && part != 0)
@@ -376,7 +432,7 @@ __global__ void stats_kernel(const DepCounters* ctr, const float4* block_stats, 
   __shared__ ff s_a[32], s_b[32];
   ff a{0.f, 0.f}, b{0.f, 0.f};
   for (int k = threadIdx.x; k < nblocks; k += blockDim.x) {
-    float4 v = block_stats[k];
+    const float4 v = block_stats[k];
     a = ff_add(a, ff{v.x, v.y});
     b = ff_add(b, ff{v.z, v.w});
   }
@@ -401,7 +457,7 @@ __global__ void stats_kernel(const DepCounters* ctr, const float4* block_stats, 
 }
 
 struct DepLayout {
-  int tdim, nt, ntiles, maxrep, nblocks;
+  int tdim, tshift, nt, ntiles, maxrep, nblocks;
   size_t scan_bytes;
   size_t total;
 };
@@ -413,7 +469,7 @@ int max_tiles_axis(int N, int tdim, int width) {
   for (int s = 0; s < N; ++s) {
     int seen[8], ns = 0;
     for (int r = 0; r < width; ++r) {
-      int t = ((s + r) % N) / tdim;
+      const int t = ((s + r) % N) / tdim;
       bool dup = false;
       for (int k = 0; k < ns; ++k) dup = dup || seen[k] == t;
       if (!dup && ns < 8) seen[ns++] = t;
@@ -427,13 +483,16 @@ int deposit_layout(int64_t n, int N, int mas, int interlace, int compat, DepLayo
   if (N < 1 || N > 4096) return GBP_ERR_INVALID;
   if (n < 0) return GBP_ERR_INVALID;
   if (mas < GBP_NGP || mas > GBP_PCS) return GBP_ERR_INVALID;
+  if (compat < 0 || compat > GBP_COMPAT_SCAN) return GBP_ERR_INVALID;
   if (compat && (mas != GBP_CIC || interlace)) return GBP_ERR_INVALID;
   L.tdim = N < TILE ? N : TILE;
+  L.tshift = (L.tdim & (L.tdim - 1)) == 0 ? __builtin_ctz(L.tdim) : -1;
   L.nt = (N + L.tdim - 1) / L.tdim;
   L.ntiles = L.nt * L.nt * L.nt;
   const int R = compat ? 2 : mas;
   const int width = R + (interlace ? 1 : 0);
   const int m = max_tiles_axis(N, L.tdim, width);
+  if (m > 3) return GBP_ERR_UNSUPPORTED;
   L.maxrep = m * m * m;
   if ((double)n * L.maxrep >= 4294967295.0) return GBP_ERR_UNSUPPORTED;
   L.nblocks = (int)((n + (long long)CNT_THREADS * CNT_ITEMS - 1) / ((long long)CNT_THREADS * CNT_ITEMS));
@@ -442,6 +501,43 @@ int deposit_layout(int64_t n, int N, int mas, int interlace, int compat, DepLayo
   L.total = align256(sizeof(DepCounters)) + align256((size_t)L.ntiles * 4) * 2 +
             align256((size_t)(L.nblocks > 0 ? L.nblocks : 1) * sizeof(float4)) +
             align256((size_t)n * L.maxrep * sizeof(float4) + 16) + align256(L.scan_bytes);
+  return GBP_OK;
+}
+
+struct Launch {
+  DepGeom g;
+  const DepLayout* L;
+  unsigned* counts;
+  unsigned* cursors;
+  DepCounters* ctr;
+  float4* block_stats;
+  float4* entries;
+  void* scan_tmp;
+  const float* mesh_in;
+  float* mesh_out;
+  cudaStream_t stream;
+};
+
+template <int MAS, int G, int CM>
+int run_scheme(const Launch& q) {
+  const DepLayout& L = *q.L;
+  if (L.nblocks > 0) {
+    count_kernel<MAS, G, CM><<<L.nblocks, CNT_THREADS, 0, q.stream>>>(q.g, q.counts, q.ctr, q.block_stats);
+    GBP_LAUNCH_CHECK();
+  }
+  size_t scan_bytes = L.scan_bytes;
+  GBP_CUDA_TRY(cub::DeviceScan::ExclusiveSum(q.scan_tmp, scan_bytes, q.counts, q.cursors, L.ntiles, q.stream));
+  if (L.nblocks > 0) {
+    scatter_kernel<MAS, G, CM><<<L.nblocks, CNT_THREADS, 0, q.stream>>>(q.g, q.cursors, q.entries);
+    GBP_LAUNCH_CHECK();
+  }
+  const size_t smem = (size_t)G * TILE3 * sizeof(long long);
+  // more than 48 KB of dynamic shared memory needs the opt-in (cheap, per call)
+  GBP_CUDA_TRY(cudaFuncSetAttribute(deposit_kernel<MAS, G, CM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem));
+  deposit_kernel<MAS, G, CM><<<L.ntiles, DEP_THREADS, smem, q.stream>>>(q.g, q.entries, q.counts, q.cursors,
+                                                                       q.ctr, q.mesh_in, q.mesh_out);
+  GBP_LAUNCH_CHECK();
   return GBP_OK;
 }
 
@@ -454,7 +550,7 @@ extern "C" int gbp_deposit_workspace_size(int64_t n, int N, int mas, int interla
                                           size_t* bytes) {
   if (!bytes) return GBP_ERR_INVALID;
   DepLayout L;
-  int st = deposit_layout(n, N, mas, interlace, compat, L);
+  const int st = deposit_layout(n, N, mas, interlace, compat, L);
   if (st) return st;
   *bytes = L.total;
   return GBP_OK;
@@ -472,48 +568,49 @@ extern "C" int gbp_deposit(const float* x, const float* y, const float* z, const
   if (!mesh_out) return GBP_ERR_INVALID;
   if (n > 0 && (!x || !y || !z)) return GBP_ERR_INVALID;
   if (!workspace || ws_bytes < L.total) return GBP_ERR_WORKSPACE;
-  if (compat != GBP_COMPAT_NONE && compat != GBP_COMPAT_VEC && compat != GBP_COMPAT_SCAN)
-    return GBP_ERR_INVALID;
 
   Carver cv(workspace);
-  DepCounters* ctr = cv.take<DepCounters>(1);
-  unsigned* counts = cv.take<unsigned>(L.ntiles);
-  unsigned* cursors = cv.take<unsigned>(L.ntiles);
-  float4* block_stats = cv.take<float4>(L.nblocks > 0 ? L.nblocks : 1);
-  float4* entries = cv.take<float4>((size_t)n * L.maxrep + 1);
-  void* scan_tmp = cv.take<char>(L.scan_bytes);
-
+  Launch q;
+  q.ctr = cv.take<DepCounters>(1);
+  q.counts = cv.take<unsigned>(L.ntiles);
+  q.cursors = cv.take<unsigned>(L.ntiles);
+  q.block_stats = cv.take<float4>(L.nblocks > 0 ? L.nblocks : 1);
+  q.entries = cv.take<float4>((size_t)n * L.maxrep + 1);
+  q.scan_tmp = cv.take<char>(L.scan_bytes);
+  q.L = &L;
+  q.mesh_in = mesh_in;
+  q.mesh_out = mesh_out;
+  q.stream = stream;
   const int G = interlace ? 2 : 1;
-  DepGeom g;
+  DepGeom& g = q.g;
   g.x = x; g.y = y; g.z = z; g.w = w; g.n = n;
   g.ox = xmin; g.oy = ymin; g.oz = zmin; g.inv_cell = inv_cell;
-  g.N = N; g.mas = mas; g.G = G; g.compat = compat; g.wrap = wrap ? 1 : 0;
-  g.tdim = L.tdim; g.nt = L.nt;
+  g.N = N; g.wrap = wrap ? 1 : 0;
+  g.tdim = L.tdim; g.tshift = L.tshift; g.nt = L.nt;
+  g.vec_ok = ((reinterpret_cast<uintptr_t>(mesh_out) | reinterpret_cast<uintptr_t>(mesh_in)) & 15u) == 0;
 
   // counters + tile counts are adjacent: one memset clears both.
-  GBP_CUDA_TRY(cudaMemsetAsync(ctr, 0, align256(sizeof(DepCounters)) + align256((size_t)L.ntiles * 4), stream));
-  if (L.nblocks > 0) {
-    count_kernel<<<L.nblocks, CNT_THREADS, 0, stream>>>(g, counts, ctr, block_stats);
-    GBP_LAUNCH_CHECK();
-  }
-  size_t scan_bytes = L.scan_bytes;
-  if (cub::DeviceScan::ExclusiveSum(scan_tmp, scan_bytes, counts, cursors, L.ntiles, stream) != cudaSuccess)
-    return GBP_ERR_CUDA;
-  if (L.nblocks > 0) {
-    scatter_kernel<<<L.nblocks, CNT_THREADS, 0, stream>>>(g, cursors, entries);
-    GBP_LAUNCH_CHECK();
-  }
-  const size_t smem = (size_t)G * TILE3 * sizeof(long long);
-  if (G == 2) {
-    // 64 KB of dynamic shared memory needs the opt-in (per device; cheap).
-    GBP_CUDA_TRY(cudaFuncSetAttribute(deposit_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    deposit_kernel<2><<<L.ntiles, DEP_THREADS, smem, stream>>>(g, entries, counts, cursors, ctr, mesh_in, mesh_out);
+  GBP_CUDA_TRY(cudaMemsetAsync(q.ctr, 0, align256(sizeof(DepCounters)) + align256((size_t)L.ntiles * 4), stream));
+  if (compat == GBP_COMPAT_VEC) st = run_scheme<GBP_CIC, 1, GBP_COMPAT_VEC>(q);
+  else if (compat == GBP_COMPAT_SCAN) st = run_scheme<GBP_CIC, 1, GBP_COMPAT_SCAN>(q);
+  else if (G == 1) {
+    switch (mas) {
+      case GBP_NGP: st = run_scheme<GBP_NGP, 1, 0>(q); break;
+      case GBP_CIC: st = run_scheme<GBP_CIC, 1, 0>(q); break;
+      case GBP_TSC: st = run_scheme<GBP_TSC, 1, 0>(q); break;
+      default: st = run_scheme<GBP_PCS, 1, 0>(q); break;
+    }
   } else {
-    deposit_kernel<1><<<L.ntiles, DEP_THREADS, smem, stream>>>(g, entries, counts, cursors, ctr, mesh_in, mesh_out);
+    switch (mas) {
+      case GBP_NGP: st = run_scheme<GBP_NGP, 2, 0>(q); break;
+      case GBP_CIC: st = run_scheme<GBP_CIC, 2, 0>(q); break;
+      case GBP_TSC: st = run_scheme<GBP_TSC, 2, 0>(q); break;
+      default: st = run_scheme<GBP_PCS, 2, 0>(q); break;
+    }
   }
-  GBP_LAUNCH_CHECK();
+  if (st) return st;
   if (stats_out) {
-    stats_kernel<<<1, 256, 0, stream>>>(ctr, block_stats, L.nblocks, n, compat, G, stats_out);
+    stats_kernel<<<1, 256, 0, stream>>>(q.ctr, q.block_stats, L.nblocks, n, compat, G, stats_out);
     GBP_LAUNCH_CHECK();
   }
   return GBP_OK;

@@ -18,5 +18,7 @@ struct gbp_bins_s {
   int* d_lut;           // [lut_n]
   float* d_inv_sinc2;   // [N/2 + 1]  1 / sinc(pi k / N)^2
   float2* d_eph;        // [N/2 + 1]  exp(i pi k / N)
+  long long* d_nmodes;  // [nb] modes per bin (geometry only, computed once)
+  double* d_ksum;       // [nb] sum of |k| per bin, grid units
   void* d_block;        // the single device allocation holding the above
 };

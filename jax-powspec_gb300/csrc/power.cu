@@ -2,22 +2,33 @@
 // |delta_k|^2 x Legendre L_l(mu) (line of sight z) and k-shell binning.
 //
 // Layout: a spectrum is complex64 [N][N][Lz] with Lz = N/2+1 (cuFFT R2C).
-// Each warp walks a contiguous run of that flat array, 32 modes per step
-// (coalesced 8-byte loads).  Along a z pencil |k| grows with kz, so the
-// 32 bins of a step form sorted runs; a warp-shuffle segmented scan sums
-// each run and its last lane adds the run total to the warp's private
-// float32 bins in shared memory.  Runs of different pencils in one step can
-// share a bin, so the adds are issued pencil by pencil with __syncwarp()
-// between them: no shared-memory atomics, a fixed order, bitwise
-// reproducible results.  At the end each CTA folds its warps' bins into a
-// float-float (hi, lo) partial, and power_reduce_kernel folds the CTAs'
-// partials in a fixed order into double totals.  (GB300 runs FP64 at a
-// small fraction of FP32 throughput, so doubles appear only in the totals.)
+// Each warp walks a contiguous run of that flat array.  Along a z pencil |k|
+// grows with kz, so consecutive modes form sorted runs of equal bin:
+//
+//  * main kernel (even N >= 64): a lane owns 4 consecutive modes per step
+//    (two 16-byte loads per grid, next step prefetched).  It sums its own
+//    runs, then one warp-shuffle segmented scan joins runs that continue
+//    across lanes.  Every maximal run is added exactly once, by the lane
+//    where it ends, to the warp's private float32 bins in shared memory.
+//  * simple kernel (odd or small N): one mode per lane and step, same scan.
+//
+// Runs of different pencils in one step can share a bin, so the adds are
+// issued pencil by pencil with __syncwarp() between them: no shared-memory
+// atomics, a fixed order, bitwise reproducible results.  At the end each CTA
+// folds its warps' bins into a float-float (hi, lo) partial, and
+// power_reduce_kernel folds the CTAs' partials in a fixed order into
+// doubles.  (GB300 runs FP64 at a small fraction of its FP32 rate, so
+// doubles appear only in the final per-bin totals.)
+//
+// The kernels accumulate the moments sum p, sum p mu^2, sum p mu^4 with
+// p = |delta|^2 W^2; the reduction turns them into the Legendre sums
+// L_0 = 1, L_2 = (3 mu^2 - 1)/2, L_4 = (35 mu^4 - 30 mu^2 + 3)/8
+// (src/correlations.py:45-47).  Mode counts and sum |k| per bin depend only
+// on the grid and come from the bin plan.
 //
 // Bin membership uses integer thresholds on k2 = kx^2+ky^2+kz^2 computed on
 // the host (gbp_bin_thresholds), which reproduces jnp.histogram applied to
-// k = sqrtf((float)k2) exactly, so mode counts match the reference bit for
-// bit (src/correlations.py:34,42,45-48).
+// k = sqrtf((float)k2) exactly (src/correlations.py:34,42,45-48).
 #include <math.h>
 
 #include <algorithm>
@@ -28,7 +39,7 @@
 namespace gbp {
 namespace {
 
-constexpr int POW_MAX_WARPS = 8;
+constexpr int POW_WARPS = 8;
 
 struct PowGeom {
   const float2* s0;
@@ -44,9 +55,8 @@ struct PowGeom {
   const int* lut;           // [lut_n]
   const float* inv_sinc2;   // [N/2+1] 1/sinc(pi k/N)^2
   const float2* eph;        // [N/2+1] exp(i pi k / N)
-  const double* mass;       // nullable
-  float2* part_ff;          // [C][NVT][nbe]
-  long long* part_cnt;      // [C][nbe]
+  int zero_dc;              // density mesh: delta(k=0) = 0 exactly
+  float2* part_ff;          // [C][NV][nbe]
   int warps;
 };
 
@@ -56,7 +66,7 @@ struct SmemPlan {
 
 __host__ __device__ inline size_t a16(size_t b) { return (b + 15) & ~size_t(15); }
 
-__host__ __device__ inline SmemPlan smem_plan(int N, int nbe, int lut_n, int warps, int NVT) {
+__host__ __device__ inline SmemPlan smem_plan(int N, int nbe, int lut_n, int warps, int NV) {
   SmemPlan p;
   const int h = N / 2;
   p.c2 = 0;
@@ -64,38 +74,279 @@ __host__ __device__ inline SmemPlan smem_plan(int N, int nbe, int lut_n, int war
   p.thr = p.eph + a16((size_t)(h + 1) * 8);
   p.lut = p.thr + a16((size_t)(nbe + 1) * 4);
   p.bins = p.lut + a16((size_t)lut_n * 4);
-  p.total = p.bins + (size_t)warps * (NVT + 1) * nbe * 4;
+  p.total = p.bins + (size_t)warps * NV * nbe * 4;
   return p;
 }
 
-template <int NV, bool KS, bool INTER>
-__global__ void __launch_bounds__(POW_MAX_WARPS * 32)
-power_kernel(PowGeom g) {
-  constexpr int NVT = NV + (KS ? 1 : 0);
-  extern __shared__ __align__(16) unsigned char smem[];
-  const SmemPlan sp = smem_plan(g.N, g.nbe, g.lut_n, g.warps, NVT);
+struct Smem {
+  float* c2;
+  float2* eph;
+  int* thr;
+  int* lut;
+  float* wbase;
+};
+
+template <int NV, bool INTER>
+__device__ __forceinline__ Smem load_tables(const PowGeom& g, unsigned char* smem) {
+  const SmemPlan sp = smem_plan(g.N, g.nbe, g.lut_n, g.warps, NV);
+  Smem s;
+  s.c2 = reinterpret_cast<float*>(smem + sp.c2);
+  s.eph = reinterpret_cast<float2*>(smem + sp.eph);
+  s.thr = reinterpret_cast<int*>(smem + sp.thr);
+  s.lut = reinterpret_cast<int*>(smem + sp.lut);
+  s.wbase = reinterpret_cast<float*>(smem + sp.bins);
   const int h = g.N / 2;
-  float* c2 = reinterpret_cast<float*>(smem + sp.c2);
-  float2* eph = reinterpret_cast<float2*>(smem + sp.eph);
-  int* thr = reinterpret_cast<int*>(smem + sp.thr);
-  int* lut = reinterpret_cast<int*>(smem + sp.lut);
-  float* wbase = reinterpret_cast<float*>(smem + sp.bins);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int stride_w = (NVT + 1) * g.nbe;
-  float* wb = wbase + warp * stride_w;                          // [NVT][nbe]
-  int* wc = reinterpret_cast<int*>(wb + NVT * g.nbe);           // [nbe]
-
   for (int k = threadIdx.x; k <= h; k += blockDim.x) {
-    float r = g.inv_sinc2[k], c = 1.0f;
-    for (int p = 0; p < g.mas_order; ++p) c *= r;               // sinc^(-2 p)
-    c2[k] = c;
-    if (INTER) eph[k] = g.eph[k];
+    const float r = g.inv_sinc2[k];
+    float c = INTER ? 0.25f : 1.0f;             // interlacing averages two grids: |(a+b)/2|^2
+    for (int p = 0; p < g.mas_order; ++p) c *= r;  // sinc^(-2 mas_order)
+    s.c2[k] = c;
+    if (INTER) s.eph[k] = g.eph[k];
   }
-  for (int k = threadIdx.x; k <= g.nbe; k += blockDim.x) thr[k] = g.thr[k];
-  for (int k = threadIdx.x; k < g.lut_n; k += blockDim.x) lut[k] = g.lut[k];
-  for (int k = threadIdx.x; k < g.warps * stride_w; k += blockDim.x) wbase[k] = 0.0f;  // int 0 == float 0 bits
+  for (int k = threadIdx.x; k <= g.nbe; k += blockDim.x) s.thr[k] = g.thr[k];
+  for (int k = threadIdx.x; k < g.lut_n; k += blockDim.x) s.lut[k] = g.lut[k];
+  for (int k = threadIdx.x; k < g.warps * NV * g.nbe; k += blockDim.x) s.wbase[k] = 0.0f;
   __syncthreads();
+  return s;
+}
 
+// Bin of k2 (>= 0), or -1 when outside the edges.
+__device__ __forceinline__ int bin_of(const PowGeom& g, const Smem& s, int k2) {
+  if (k2 > g.tu) return -1;
+  int r = s.lut[k2 >> g.lut_shift];
+  while (r <= g.nbe && s.thr[r] <= k2) ++r;
+  return min(min(r, g.nb), g.nbe) - 1;          // r <= nbe whenever nbe < nb; the clamp only guards
+}
+
+// Per-pencil constants: signed (kx, ky), window of x and y, interlacing phase.
+struct Pencil {
+  int kp2;
+  float cxy;
+  float pr, pi;
+};
+
+template <bool INTER>
+__device__ __forceinline__ Pencil pencil_of(const PowGeom& g, const Smem& s, int ix, int iy) {
+  const int kx = signed_k(ix, g.N), ky = signed_k(iy, g.N);
+  const int ax = kx < 0 ? -kx : kx, ay = ky < 0 ? -ky : ky;
+  Pencil p;
+  p.kp2 = kx * kx + ky * ky;
+  p.cxy = s.c2[ax] * s.c2[ay];
+  p.pr = 1.0f;
+  p.pi = 0.0f;
+  if (INTER) {  // exp(i pi (kx+ky)/N) from the |k| table (conjugate for k < 0)
+    float2 ex = s.eph[ax], ey = s.eph[ay];
+    if (kx < 0) ex.y = -ex.y;
+    if (ky < 0) ey.y = -ey.y;
+    p.pr = ex.x * ey.x - ex.y * ey.y;
+    p.pi = ex.x * ey.y + ex.y * ey.x;
+  }
+  return p;
+}
+
+// One mode: its moments (p, p mu^2, p mu^4) and its k2.  The window of z,
+// the factor 1/4 of the interlaced average and the pencil's x,y window are
+// folded into c2 / cxy.
+template <int NV, bool INTER>
+__device__ __forceinline__ void mode_moments(const Smem& s, const Pencil& pc, int kz, float2 a, float2 b,
+                                             bool zero, float (&v)[NV], int& k2) {
+  float re = a.x, im = a.y;
+  if (INTER) {
+    const float2 ez = s.eph[kz];
+    const float qr = pc.pr * ez.x - pc.pi * ez.y;
+    const float qi = pc.pr * ez.y + pc.pi * ez.x;
+    re = a.x + (b.x * qr - b.y * qi);
+    im = a.y + (b.x * qi + b.y * qr);
+  }
+  if (zero) re = im = 0.0f;
+  k2 = pc.kp2 + kz * kz;
+  const float p = (re * re + im * im) * (pc.cxy * s.c2[kz]);
+  v[0] = p;
+  if (NV > 1) {
+    const float mu2 = k2 > 0 ? __fdividef((float)(kz * kz), (float)k2) : 0.0f;
+    v[1] = p * mu2;
+    if (NV > 2) v[2] = v[1] * mu2;
+  }
+}
+
+// Warp-inclusive segmented scan (segments start at lanes whose head flag is set).
+template <int NV>
+__device__ __forceinline__ void seg_scan(float (&v)[NV], unsigned heads, int lane) {
+  const int segstart = 31 - __clz(heads & (0xffffffffu >> (31 - lane)));
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const bool take = lane - d >= segstart;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+      const float t = __shfl_up_sync(0xffffffffu, v[q], d);
+      if (take) v[q] += t;
+    }
+  }
+}
+
+template <int NV>
+__device__ __forceinline__ void bin_add(float* wb, int nbe, int bin, const float (&v)[NV]) {
+#pragma unroll
+  for (int q = 0; q < NV; ++q) wb[q * nbe + bin] += v[q];
+}
+
+template <int NV>
+__device__ __forceinline__ void cta_fold(const PowGeom& g, const Smem& s) {
+  __syncthreads();
+  float2* pf = g.part_ff + (long long)blockIdx.x * NV * g.nbe;
+  for (int b = threadIdx.x; b < g.nbe; b += blockDim.x) {
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+      ff acc{0.f, 0.f};
+      for (int w = 0; w < g.warps; ++w) acc = ff_add_f(acc, s.wbase[(w * NV + q) * g.nbe + b]);
+      pf[q * g.nbe + b] = make_float2(acc.hi, acc.lo);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Main kernel: 4 modes per lane, 128 per warp step.  Requires even N (so that
+// both grids' arrays are 16-byte aligned and every lane's 4 modes are either
+// all in range or all out) and a chunk that is a multiple of 128.
+template <int NV, bool INTER>
+__global__ void __launch_bounds__(POW_WARPS * 32)
+power_kernel4(PowGeom g) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const Smem s = load_tables<NV, INTER>(g, smem);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float* wb = s.wbase + warp * NV * g.nbe;
+  const long long wglob = (long long)blockIdx.x * g.warps + warp;
+  const long long beg = wglob * g.chunk;
+  const long long end = min(beg + g.chunk, g.total);
+
+  if (beg < end) {
+    // first mode of this lane in the current step, and its pencil / kz
+    long long f = beg + 4 * lane;
+    long long pen = f / g.Lz;
+    int kz = (int)(f - pen * g.Lz);
+    int iy = (int)(pen % g.N);
+    int ix = (int)(pen / g.N);
+    const float4* s0 = reinterpret_cast<const float4*>(g.s0);
+    const float4* s1 = reinterpret_cast<const float4*>(g.s1);
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 a01 = z4, a23 = z4, b01 = z4, b23 = z4;
+    if (f < end) {
+      a01 = __ldcs(s0 + f / 2);
+      a23 = __ldcs(s0 + f / 2 + 1);
+      if (INTER) { b01 = __ldcs(s1 + f / 2); b23 = __ldcs(s1 + f / 2 + 1); }
+    }
+    for (long long fb = beg; fb < end; fb += 128) {
+      const bool valid = f < end;
+      // prefetch the next step
+      const long long fn = f + 128;
+      float4 na01 = z4, na23 = z4, nb01 = z4, nb23 = z4;
+      if (fn < end) {
+        na01 = __ldcs(s0 + fn / 2);
+        na23 = __ldcs(s0 + fn / 2 + 1);
+        if (INTER) { nb01 = __ldcs(s1 + fn / 2); nb23 = __ldcs(s1 + fn / 2 + 1); }
+      }
+      const float2 A[4] = {make_float2(a01.x, a01.y), make_float2(a01.z, a01.w), make_float2(a23.x, a23.y),
+                           make_float2(a23.z, a23.w)};
+      const float2 Bv[4] = {make_float2(b01.x, b01.y), make_float2(b01.z, b01.w), make_float2(b23.x, b23.y),
+                            make_float2(b23.z, b23.w)};
+      // per-mode moments, bins and pencil ids (4 consecutive modes)
+      float P[4][NV];          // running in-lane run sums
+      int bin[4], pid[4];
+      {
+        int cix = ix, ciy = iy, ckz = kz;
+        Pencil pc = pencil_of<INTER>(g, s, cix, ciy);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          if (j > 0 && ++ckz == g.Lz) {
+            ckz = 0;
+            if (++ciy == g.N) { ciy = 0; ++cix; }
+            pc = pencil_of<INTER>(g, s, cix, ciy);
+          }
+          pid[j] = cix * g.N + ciy;
+          int k2;
+          const bool zero = g.zero_dc && (f + j == 0);
+          mode_moments<NV, INTER>(s, pc, ckz, A[j], Bv[j], zero, P[j], k2);
+          bin[j] = valid ? bin_of(g, s, k2) : -1;
+        }
+      }
+      // in-lane runs: P[j] becomes the sum of the run up to mode j
+      bool start[4];
+      start[0] = true;
+#pragma unroll
+      for (int j = 1; j < 4; ++j) {
+        start[j] = (bin[j] != bin[j - 1]) || (pid[j] != pid[j - 1]);
+        if (!start[j]) {
+#pragma unroll
+          for (int q = 0; q < NV; ++q) P[j][q] += P[j - 1][q];
+        }
+      }
+      const bool multi = start[1] || start[2] || start[3];
+      // run keys: pencil relative to lane 0's first mode, and bin
+      const int p0 = __shfl_sync(0xffffffffu, pid[0], 0);
+      const int key_first = ((pid[0] - p0) << 20) | (bin[0] + 1);
+      const int key_last = ((pid[3] - p0) << 20) | (bin[3] + 1);
+      const int prev_last = __shfl_up_sync(0xffffffffu, key_last, 1);
+      const bool cont = lane > 0 && key_first == prev_last;       // first run continues the previous lane's last
+      const unsigned heads = __ballot_sync(0xffffffffu, multi || !cont);
+      float T[NV];
+#pragma unroll
+      for (int q = 0; q < NV; ++q) T[q] = P[3][q];
+      seg_scan<NV>(T, heads, lane);
+      float Tprev[NV];
+#pragma unroll
+      for (int q = 0; q < NV; ++q) Tprev[q] = __shfl_up_sync(0xffffffffu, T[q], 1);
+      const bool next_cont = __shfl_down_sync(0xffffffffu, cont, 1) && lane < 31;
+      // run ends inside the lane (j < 3); the first one absorbs the carry
+      bool endin[3];
+      int firstend = 3;
+#pragma unroll
+      for (int j = 2; j >= 0; --j) {
+        endin[j] = start[j + 1];
+        if (endin[j]) firstend = j;
+      }
+      if (cont && multi) {
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+          if (j == firstend) {
+#pragma unroll
+            for (int q = 0; q < NV; ++q) P[j][q] += Tprev[q];
+          }
+      }
+      const bool flush_last = !next_cont;
+      // flush pencil by pencil
+      const int rel0 = pid[0] - p0, rel3 = pid[3] - p0;
+      const int nph = __reduce_max_sync(0xffffffffu, valid ? rel3 : 0) + 1;   // pencils in this step
+      for (int ph = 0; ph < nph; ++ph) {
+        if (rel0 <= ph && ph <= rel3) {
+#pragma unroll
+          for (int j = 0; j < 3; ++j)
+            if (endin[j] && bin[j] >= 0 && pid[j] - p0 == ph) bin_add<NV>(wb, g.nbe, bin[j], P[j]);
+          if (flush_last && bin[3] >= 0 && rel3 == ph) bin_add<NV>(wb, g.nbe, bin[3], T);
+        }
+        __syncwarp();
+      }
+      // advance
+      a01 = na01; a23 = na23; b01 = nb01; b23 = nb23;
+      f += 128;
+      kz += 128;
+      while (kz >= g.Lz) {
+        kz -= g.Lz;
+        if (++iy == g.N) { iy = 0; ++ix; }
+      }
+    }
+  }
+  cta_fold<NV>(g, s);
+}
+
+// ---------------------------------------------------------------------------
+// Simple kernel: one mode per lane per step (any N, any alignment).
+template <int NV, bool INTER>
+__global__ void __launch_bounds__(POW_WARPS * 32)
+power_kernel1(PowGeom g) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const Smem s = load_tables<NV, INTER>(g, smem);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float* wb = s.wbase + warp * NV * g.nbe;
   const long long wglob = (long long)blockIdx.x * g.warps + warp;
   const long long beg = wglob * g.chunk;
   const long long end = min(beg + g.chunk, g.total);
@@ -105,81 +356,29 @@ power_kernel(PowGeom g) {
     int kz = (int)(f - pen * g.Lz);
     int iy = (int)(pen % g.N);
     int ix = (int)(pen / g.N);
-    const double m0 = g.mass ? g.mass[0] : 0.0;
-    const double m1 = (g.mass && INTER) ? g.mass[1] : 0.0;
-
     for (long long fb = beg; fb < end; fb += 32) {
       const bool valid = f < end;
-      float v[NVT];
+      float v[NV];
 #pragma unroll
-      for (int q = 0; q < NVT; ++q) v[q] = 0.0f;
+      for (int q = 0; q < NV; ++q) v[q] = 0.0f;
       int bin = -1;
       if (valid) {
-        const int kx = signed_k(ix, g.N), ky = signed_k(iy, g.N);
-        const int ax = kx < 0 ? -kx : kx, ay = ky < 0 ? -ky : ky;
-        const int k2 = kx * kx + ky * ky + kz * kz;
-        float2 a = g.s0[f];
-        float re, im;
-        if (INTER) {
-          float2 b = g.s1[f];
-          if (f == 0 && g.mass) {
-            a.x = (float)((double)a.x - m0);
-            b.x = (float)((double)b.x - m1);
-          }
-          // exp(i pi (kx+ky+kz)/N) from the |k| table (conjugate for k < 0)
-          float2 ex = eph[ax], ey = eph[ay], ez = eph[kz];
-          if (kx < 0) ex.y = -ex.y;
-          if (ky < 0) ey.y = -ey.y;
-          const float pr = ex.x * ey.x - ex.y * ey.y;
-          const float pi = ex.x * ey.y + ex.y * ey.x;
-          const float qr = pr * ez.x - pi * ez.y;
-          const float qi = pr * ez.y + pi * ez.x;
-          re = 0.5f * (a.x + (b.x * qr - b.y * qi));
-          im = 0.5f * (a.y + (b.x * qi + b.y * qr));
-        } else {
-          if (f == 0 && g.mass) a.x = (float)((double)a.x - m0);
-          re = a.x;
-          im = a.y;
-        }
-        const float p = (re * re + im * im) * (c2[ax] * c2[ay] * c2[kz]);
-        v[0] = p;
-        if (NV > 1) {
-          const float mu2 = k2 > 0 ? __fdividef((float)(kz * kz), (float)k2) : 0.0f;
-          v[1] = p * (1.5f * mu2 - 0.5f);
-          if (NV > 2) v[2] = p * ((4.375f * mu2 - 3.75f) * mu2 + 0.375f);
-        }
-        if (KS) v[NV] = sqrtf((float)k2);
-        if (k2 <= g.tu) {
-          int r = lut[k2 >> g.lut_shift];
-          while (r <= g.nbe && thr[r] <= k2) ++r;
-          bin = min(min(r, g.nb), g.nbe) - 1;   // r <= nbe whenever nbe < nb; the clamp only guards
-        }
+        const Pencil pc = pencil_of<INTER>(g, s, ix, iy);
+        const float2 a = g.s0[f];
+        const float2 b = INTER ? g.s1[f] : make_float2(0.f, 0.f);
+        int k2;
+        mode_moments<NV, INTER>(s, pc, kz, a, b, g.zero_dc && f == 0, v, k2);
+        bin = bin_of(g, s, k2);
       }
-      // segmented inclusive scan over runs of equal bin
       const int bprev = __shfl_up_sync(0xffffffffu, bin, 1);
-      const bool head = (lane == 0) || (bin != bprev);
-      const unsigned hm = __ballot_sync(0xffffffffu, head);
-      const int segstart = 31 - __clz(hm & (0xffffffffu >> (31 - lane)));
-#pragma unroll
-      for (int d = 1; d < 32; d <<= 1) {
-        const bool take = lane - d >= segstart;
-#pragma unroll
-        for (int q = 0; q < NVT; ++q) {
-          const float t = __shfl_up_sync(0xffffffffu, v[q], d);
-          if (take) v[q] += t;
-        }
-      }
-      const bool segend = (lane == 31) || ((hm >> (lane + 1)) & 1u);
-      // flush pencil by pencil (a bin can repeat only across pencils)
+      const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || bin != bprev);
+      seg_scan<NV>(v, heads, lane);
+      const bool segend = (lane == 31) || ((heads >> (lane + 1)) & 1u);
       const int pid = ix * g.N + iy;
       const int rel = pid - __shfl_sync(0xffffffffu, pid, 0);
       const int nph = __shfl_sync(0xffffffffu, rel, 31) + 1;
       for (int ph = 0; ph < nph; ++ph) {
-        if (segend && bin >= 0 && rel == ph) {
-#pragma unroll
-          for (int q = 0; q < NVT; ++q) wb[q * g.nbe + bin] += v[q];
-          wc[bin] += lane - segstart + 1;
-        }
+        if (segend && bin >= 0 && rel == ph) bin_add<NV>(wb, g.nbe, bin, v);
         __syncwarp();
       }
       f += 32;
@@ -190,54 +389,38 @@ power_kernel(PowGeom g) {
       }
     }
   }
-  __syncthreads();
-
-  // CTA fold: warps in order, float-float; counts in int64.
-  float2* pf = g.part_ff + (long long)blockIdx.x * NVT * g.nbe;
-  long long* pc = g.part_cnt + (long long)blockIdx.x * g.nbe;
-  for (int b = threadIdx.x; b < g.nbe; b += blockDim.x) {
-#pragma unroll
-    for (int q = 0; q < NVT; ++q) {
-      ff s{0.f, 0.f};
-      for (int w = 0; w < g.warps; ++w) s = ff_add_f(s, wbase[w * stride_w + q * g.nbe + b]);
-      pf[q * g.nbe + b] = make_float2(s.hi, s.lo);
-    }
-    long long c = 0;
-    for (int w = 0; w < g.warps; ++w) c += reinterpret_cast<const int*>(wbase + w * stride_w + NVT * g.nbe)[b];
-    pc[b] = c;
-  }
+  cta_fold<NV>(g, s);
 }
 
-// One warp per bin: fold the CTA partials (fixed order) into doubles.
-__global__ void power_reduce_kernel(const float2* __restrict__ part_ff, const long long* __restrict__ part_cnt,
-                                    int C, int NV, int KS, int nb, int nbe, double* sums_out,
-                                    long long* nmodes_out, double* ksum_out) {
+// One warp per bin: fold the CTA partials (fixed order) into double moment
+// totals and form the Legendre sums; copy the plan's geometry per bin.
+__global__ void power_reduce_kernel(const float2* __restrict__ part_ff, int C, int NV, int nb, int nbe,
+                                    const long long* __restrict__ plan_nmodes, const double* __restrict__ plan_ksum,
+                                    double* sums_out, long long* nmodes_out, double* ksum_out) {
   const int b = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (b >= nb) return;
-  const int NVT = NV + KS;
-  double tot[4] = {0.0, 0.0, 0.0, 0.0};
-  long long cnt = 0;
+  double m[3] = {0.0, 0.0, 0.0};
   if (b < nbe) {
-    for (int q = 0; q < NVT; ++q) {
-      ff s{0.f, 0.f};
+    for (int q = 0; q < NV; ++q) {
+      ff acc{0.f, 0.f};
       for (int c = lane; c < C; c += 32) {
-        const float2 v = part_ff[((long long)c * NVT + q) * nbe + b];
-        s = ff_add(s, ff{v.x, v.y});
+        const float2 v = part_ff[((long long)c * NV + q) * nbe + b];
+        acc = ff_add(acc, ff{v.x, v.y});
       }
       for (int o = 16; o > 0; o >>= 1) {
-        ff t{__shfl_xor_sync(0xffffffffu, s.hi, o), __shfl_xor_sync(0xffffffffu, s.lo, o)};
-        s = ff_add(s, t);
+        ff t{__shfl_xor_sync(0xffffffffu, acc.hi, o), __shfl_xor_sync(0xffffffffu, acc.lo, o)};
+        acc = ff_add(acc, t);
       }
-      tot[q] = (double)s.hi + (double)s.lo;
+      m[q] = (double)acc.hi + (double)acc.lo;
     }
-    for (int c = lane; c < C; c += 32) cnt += part_cnt[(long long)c * nbe + b];
-    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
   }
   if (lane == 0) {
-    for (int l = 0; l < 3; ++l) sums_out[b * 3 + l] = l < NV ? tot[l] : 0.0;
-    nmodes_out[b] = cnt;
-    if (ksum_out) ksum_out[b] = KS ? tot[NV] : 0.0;
+    sums_out[b * 3 + 0] = m[0];
+    sums_out[b * 3 + 1] = NV > 1 ? 1.5 * m[1] - 0.5 * m[0] : 0.0;
+    sums_out[b * 3 + 2] = NV > 2 ? (35.0 * m[2] - 30.0 * m[1] + 3.0 * m[0]) * 0.125 : 0.0;
+    nmodes_out[b] = plan_nmodes[b];
+    if (ksum_out) ksum_out[b] = plan_ksum[b];
   }
 }
 
@@ -255,7 +438,7 @@ __global__ void power_normalize_kernel(const double* sums, const long long* nmod
   }
   const double n = (double)nmodes[b];
   for (int l = 0; l < 3; ++l) {
-    double p = (4.0 * l + 1.0) * sums[b * 3 + l] / n * norm;  // 0/0 -> NaN, as the reference
+    double p = (4.0 * l + 1.0) * sums[b * 3 + l] / n * norm;  // (2 ell + 1); 0/0 -> NaN like the reference
     if (l == 0) p -= shot;
     pk_out[b * 3 + l] = p;
   }
@@ -263,30 +446,31 @@ __global__ void power_normalize_kernel(const double* sums, const long long* nmod
 }
 
 struct PowLayout {
-  int NV, KS, warps, C;
+  int NV, warps, C;
+  bool wide;                // the 4-modes-per-lane kernel
   long long total, chunk;
   size_t smem, ws_total;
 };
 
 // A pure function of (N, bins, ells): the summation order, and therefore the
 // result, is the same on every device.
-int power_layout(const gbp_bins_s* B, int ells, PowLayout& L) {
+int power_layout(const gbp_bins_s* B, int G, int ells, PowLayout& L) {
   L.NV = (ells & GBP_ELL4) ? 3 : ((ells & GBP_ELL2) ? 2 : 1);
-  L.KS = (ells & GBP_KSUM) ? 1 : 0;
-  const int NVT = L.NV + L.KS;
   const size_t budget = 200 * 1024;
-  int w = POW_MAX_WARPS;
-  while (w > 1 && smem_plan(B->N, B->nbe, B->lut_n, w, NVT).total > budget) --w;
-  L.smem = smem_plan(B->N, B->nbe, B->lut_n, w, NVT).total;
+  int w = POW_WARPS;
+  while (w > 1 && smem_plan(B->N, B->nbe, B->lut_n, w, L.NV).total > budget) --w;
+  L.smem = smem_plan(B->N, B->nbe, B->lut_n, w, L.NV).total;
   if (L.smem > budget) return GBP_ERR_UNSUPPORTED;
   L.warps = w;
   L.total = (long long)B->N * B->N * (B->N / 2 + 1);
+  L.wide = (B->N % 2 == 0) && B->N >= 64;
   long long target = L.total / (8LL * 152 * 4);
-  target = std::max(1024LL, std::min(8192LL, target));
-  L.chunk = (target + 31) & ~31LL;
+  target = std::max(1024LL, std::min(16384LL, target));
+  L.chunk = (target + 127) & ~127LL;
   const long long nw = (L.total + L.chunk - 1) / L.chunk;
   L.C = (int)((nw + w - 1) / w);
-  L.ws_total = align256((size_t)L.C * NVT * B->nbe * sizeof(float2)) + align256((size_t)L.C * B->nbe * 8);
+  L.ws_total = align256((size_t)L.C * L.NV * B->nbe * sizeof(float2));
+  (void)G;
   return GBP_OK;
 }
 
@@ -298,7 +482,7 @@ using namespace gbp;
 extern "C" int gbp_power_workspace_size(gbp_bins bins, int G, int ells, size_t* bytes) {
   if (!bins || !bytes || (G != 1 && G != 2)) return GBP_ERR_INVALID;
   PowLayout L;
-  int st = power_layout(bins, ells, L);
+  const int st = power_layout(bins, G, ells, L);
   if (st) return st;
   *bytes = L.ws_total;
   return GBP_OK;
@@ -314,13 +498,12 @@ extern "C" int gbp_power(const void* spectrum, int G, gbp_bins B, int mas_order,
   if ((ells & (GBP_ELL0 | GBP_ELL2 | GBP_ELL4)) == 0 || (ells & ~15)) return GBP_ERR_INVALID;
   if ((ells & GBP_KSUM) && !ksum_out) return GBP_ERR_INVALID;
   PowLayout L;
-  int st = power_layout(B, ells, L);
+  int st = power_layout(B, G, ells, L);
   if (st) return st;
   if (!workspace || ws_bytes < L.ws_total) return GBP_ERR_WORKSPACE;
 
   Carver cv(workspace);
-  float2* part_ff = cv.take<float2>((size_t)L.C * (L.NV + L.KS) * B->nbe);
-  long long* part_cnt = cv.take<long long>((size_t)L.C * B->nbe);
+  float2* part_ff = cv.take<float2>((size_t)L.C * L.NV * B->nbe);
 
   PowGeom g;
   g.s0 = static_cast<const float2*>(spectrum);
@@ -339,26 +522,27 @@ extern "C" int gbp_power(const void* spectrum, int G, gbp_bins B, int mas_order,
   g.lut = B->d_lut;
   g.inv_sinc2 = B->d_inv_sinc2;
   g.eph = B->d_eph;
-  g.mass = mass;
+  g.zero_dc = mass != nullptr;
   g.part_ff = part_ff;
-  g.part_cnt = part_cnt;
   g.warps = L.warps;
+  // the wide kernel reads float4s: both grids must start 16-byte aligned
+  const bool aligned = ((reinterpret_cast<uintptr_t>(g.s0) | reinterpret_cast<uintptr_t>(g.s1)) & 15u) == 0;
+  const bool wide = L.wide && aligned;
 
   void (*kern)(PowGeom) = nullptr;
   const bool inter = G == 2;
-#define GBP_PICK(NVv, KSv) kern = inter ? power_kernel<NVv, KSv, true> : power_kernel<NVv, KSv, false>;
-  if (L.KS) {
-    if (L.NV == 1) { GBP_PICK(1, true) } else if (L.NV == 2) { GBP_PICK(2, true) } else { GBP_PICK(3, true) }
-  } else {
-    if (L.NV == 1) { GBP_PICK(1, false) } else if (L.NV == 2) { GBP_PICK(2, false) } else { GBP_PICK(3, false) }
-  }
+#define GBP_PICK(NVv)                                                                               \
+  kern = wide ? (inter ? power_kernel4<NVv, true> : power_kernel4<NVv, false>)                   \
+              : (inter ? power_kernel1<NVv, true> : power_kernel1<NVv, false>);
+  if (L.NV == 1) { GBP_PICK(1) } else if (L.NV == 2) { GBP_PICK(2) } else { GBP_PICK(3) }
 #undef GBP_PICK
   GBP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem));
   kern<<<L.C, L.warps * 32, L.smem, stream>>>(g);
   GBP_LAUNCH_CHECK();
   const int wpb = 8;
   power_reduce_kernel<<<(B->nb + wpb - 1) / wpb, wpb * 32, 0, stream>>>(
-      part_ff, part_cnt, L.C, L.NV, L.KS, B->nb, B->nbe, sums_out, nmodes_out, ksum_out);
+      part_ff, L.C, L.NV, B->nb, B->nbe, B->d_nmodes, B->d_ksum, sums_out, nmodes_out,
+      (ells & GBP_KSUM) ? ksum_out : nullptr);
   GBP_LAUNCH_CHECK();
   return GBP_OK;
 }

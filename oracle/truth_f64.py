@@ -137,9 +137,11 @@ def power(meshes: np.ndarray, box_size: float, kedges_grid, mas_order: int = 2, 
     with np.errstate(invalid="ignore", divide="ignore"):
         pk = sums / nmodes[:, None] * np.array([1.0, 5.0, 9.0]) * norm
         kmean = ksum / nmodes * (2 * np.pi / L)
+    shot = 0.0
     if sum_w2 is not None:
-        pk[:, 0] -= L ** 3 * float(sum_w2) / mass ** 2
-    return {"sums": sums, "nmodes": nmodes, "ksum": ksum, "pk": pk, "kmean": kmean, "mass": mass}
+        shot = L ** 3 * float(sum_w2) / mass ** 2
+        pk[:, 0] -= shot
+    return {"sums": sums, "nmodes": nmodes, "ksum": ksum, "pk": pk, "kmean": kmean, "mass": mass, "shot": shot}
 
 
 def power_multipoles(x, y, z, w, *, box_size: float, n_mesh: int, mas: int, interlace: bool,
