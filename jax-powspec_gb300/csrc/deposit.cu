@@ -11,8 +11,10 @@
 //                      touched tile's bucket: a one-digit radix sort of the
 //                      particles by tile, replicated across tile faces.
 //   4. deposit_kernel  one CTA per tile accumulates its bucket in shared
-//                      memory in int64 fixed point (scale 2^s fixed by n and
-//                      max|w|), then writes its cells of the mesh exactly once.
+//                      memory in int64 fixed point (scale 2^s fixed by max|w|;
+//                      each add is a native 32-bit atomic on the low word plus
+//                      a carry into the high word), then writes its cells of
+//                      the mesh exactly once.
 //   5. stats_kernel    folds the per-block partial sums in a fixed order.
 //
 // Integer accumulation makes each cell's sum independent of particle order
@@ -31,7 +33,7 @@ constexpr int TILE = 16;              // tile edge (cells); >= widest stencil (5
 constexpr int TILE3 = TILE * TILE * TILE;
 constexpr int DEP_THREADS = 256;
 constexpr int CNT_THREADS = 256;
-constexpr int CNT_ITEMS = 8;          // particles per thread in count/scatter
+constexpr int CNT_ITEMS = 2;          // particles per thread in count/scatter
 constexpr float MAX_ABS_U = 1073741824.0f;  // |u| < 2^30 cells, else dropped
 
 struct DepGeom {
@@ -155,13 +157,33 @@ __device__ __forceinline__ void make_axis(const DepGeom& g, float u, int grid, A
   else axis_bspline<MAS>(u, g.N, grid, a);
 }
 
+// The particles of one thread in count/scatter: loads issued together.
+struct Batch {
+  float x[CNT_ITEMS], y[CNT_ITEMS], z[CNT_ITEMS], w[CNT_ITEMS];
+  bool in[CNT_ITEMS];
+};
+
+__device__ __forceinline__ void load_batch(const DepGeom& g, Batch& b) {
+  const long long base = (long long)blockIdx.x * CNT_THREADS * CNT_ITEMS + threadIdx.x;
+#pragma unroll
+  for (int k = 0; k < CNT_ITEMS; ++k) {
+    const long long i = base + (long long)k * CNT_THREADS;
+    b.in[k] = i < g.n;
+    if (b.in[k]) {
+      b.x[k] = __ldcs(g.x + i);
+      b.y[k] = __ldcs(g.y + i);
+      b.z[k] = __ldcs(g.z + i);
+      b.w[k] = g.w ? __ldcs(g.w + i) : 1.0f;
+    }
+  }
+}
+
 // Grid coordinate of a particle; false if it must be dropped (non-finite, or
 // so far outside the box that int32 cells would overflow).
-__device__ __forceinline__ bool grid_coords(const DepGeom& g, long long i, float u[3], float& w) {
-  u[0] = __fmul_rn(__fsub_rn(g.x[i], g.ox), g.inv_cell);
-  u[1] = __fmul_rn(__fsub_rn(g.y[i], g.oy), g.inv_cell);
-  u[2] = __fmul_rn(__fsub_rn(g.z[i], g.oz), g.inv_cell);
-  w = g.w ? g.w[i] : 1.0f;
+__device__ __forceinline__ bool grid_coords(const DepGeom& g, float x, float y, float z, float u[3]) {
+  u[0] = __fmul_rn(__fsub_rn(x, g.ox), g.inv_cell);
+  u[1] = __fmul_rn(__fsub_rn(y, g.oy), g.inv_cell);
+  u[2] = __fmul_rn(__fsub_rn(z, g.oz), g.inv_cell);
   return fabsf(u[0]) < MAX_ABS_U && fabsf(u[1]) < MAX_ABS_U && fabsf(u[2]) < MAX_ABS_U;  // false for NaN
 }
 
@@ -227,13 +249,14 @@ count_kernel(DepGeom g, unsigned* __restrict__ counts, DepCounters* ctr, float4*
   float maxw = 0.0f;
   ff sw{0.f, 0.f}, sw2{0.f, 0.f};
   unsigned kept = 0, bad = 0;
-  const long long base = (long long)blockIdx.x * CNT_THREADS * CNT_ITEMS + threadIdx.x;
-#pragma unroll 2
+  Batch bt;
+  load_batch(g, bt);
+#pragma unroll
   for (int k = 0; k < CNT_ITEMS; ++k) {
-    const long long i = base + (long long)k * CNT_THREADS;
-    if (i >= g.n) break;
-    float u[3], w;
-    if (!grid_coords(g, i, u, w)) { ++bad; continue; }
+    if (!bt.in[k]) continue;
+    float u[3];
+    const float w = bt.w[k];
+    if (!grid_coords(g, bt.x[k], bt.y[k], bt.z[k], u)) { ++bad; continue; }
     int x0, x1, x2, y0, y1, y2, z0, z1, z2;
     const int nx = axis_tiles<MAS, G, CM>(g, u[0], x0, x1, x2);
     const int ny = axis_tiles<MAS, G, CM>(g, u[1], y0, y1, y2);
@@ -281,13 +304,14 @@ count_kernel(DepGeom g, unsigned* __restrict__ counts, DepCounters* ctr, float4*
 template <int MAS, int G, int CM>
 __global__ void __launch_bounds__(CNT_THREADS)
 scatter_kernel(DepGeom g, unsigned* __restrict__ cursors, float4* __restrict__ entries) {
-  const long long base = (long long)blockIdx.x * CNT_THREADS * CNT_ITEMS + threadIdx.x;
-#pragma unroll 2
+  Batch bt;
+  load_batch(g, bt);
+#pragma unroll
   for (int k = 0; k < CNT_ITEMS; ++k) {
-    const long long i = base + (long long)k * CNT_THREADS;
-    if (i >= g.n) break;
-    float u[3], w;
-    if (!grid_coords(g, i, u, w)) continue;
+    if (!bt.in[k]) continue;
+    float u[3];
+    const float w = bt.w[k];
+    if (!grid_coords(g, bt.x[k], bt.y[k], bt.z[k], u)) continue;
     int x0, x1, x2, y0, y1, y2, z0, z1, z2;
     const int nx = axis_tiles<MAS, G, CM>(g, u[0], x0, x1, x2);
     const int ny = axis_tiles<MAS, G, CM>(g, u[1], y0, y1, y2);
@@ -303,13 +327,26 @@ scatter_kernel(DepGeom g, unsigned* __restrict__ cursors, float4* __restrict__ e
   }
 }
 
-// Fixed-point exponent: every partial sum stays below 2^61 in magnitude.
-__device__ __forceinline__ int fixed_scale_exp(long long n, unsigned maxw_bits, int compat) {
-  const double bound = (double)n * (double)__uint_as_float(maxw_bits) * (compat ? 27.0 : 1.0);
-  if (!(bound > 0.0) || !isfinite(bound)) return 0;
-  const int e = ilogb(bound) + 1;               // bound < 2^e
-  const int s = 61 - e;
-  return s < -120 ? -120 : (s > 120 ? 120 : s);
+// Fixed-point exponent s: one contribution w * W (|W| <= 1, or <= 8 for the
+// reference CIC, whose fractions can leave [0,1) off the box) is an integer
+// below 2^30 in magnitude, so it fits one 32-bit atomic on the low word; the
+// 64-bit cell sums hold n * 2^30 without overflow for any n < 2^32.
+// Float32 and integer operations only (GB300's FP64 rate is tiny).
+__device__ __forceinline__ int fixed_scale_exp(unsigned maxw_bits, int compat) {
+  const float maxw = __uint_as_float(maxw_bits);
+  if (!(maxw > 0.0f) || !(maxw < 3.0e38f)) return 0;
+  int ew;
+  frexpf(maxw, &ew);                            // maxw < 2^ew
+  const int s = 30 - ew - (compat ? 3 : 0);
+  return s < -100 ? -100 : (s > 100 ? 100 : s);
+}
+
+// int64 fixed-point value -> float32 (two exact 32-bit halves, one rounding in the FMA).
+__device__ __forceinline__ float fixed_to_float(long long q, float inv_sc) {
+  const int hi = (int)(q >> 32);
+  const unsigned lo = (unsigned)(q & 0xffffffffull);
+  const float v = __fmaf_rn(__int2float_rn(hi), 4294967296.0f, __uint2float_rn(lo));
+  return __fmul_rn(v, inv_sc);
 }
 
 // Local (in-tile) coordinate of stencil node r of an axis, or -1.
@@ -322,34 +359,45 @@ __device__ __forceinline__ void local_nodes(const Axis<R>& a, int N, int t0, int
   }
 }
 
-// Pass 4: one CTA per tile.
+// Pass 4: one CTA per tile; the grids go one after the other through the
+// same shared memory (more CTAs per SM), re-reading the bucket from L2.
+//
+// Each cell is an int64 kept as separate low and high 32-bit words
+// (consecutive cells hit consecutive banks).  A contribution is one native
+// 32-bit atomic on the low word, whose return value tells whether it carried
+// into the high word, which then gets the (rare) second atomic.  The integer
+// sums are exact whatever the order of the adds.
 template <int MAS, int G, int CM>
 __global__ void __launch_bounds__(DEP_THREADS)
 deposit_kernel(DepGeom g, const float4* __restrict__ entries, const unsigned* __restrict__ counts,
                const unsigned* __restrict__ cursors, DepCounters* ctr, const float* __restrict__ mesh_in,
                float* __restrict__ mesh_out) {
   constexpr int R = Scheme<MAS, CM>::R;
-  extern __shared__ __align__(16) long long acc[];   // [G][TILE3]
+  extern __shared__ __align__(16) unsigned acc32[];
+  unsigned* lo = acc32;
+  unsigned* hi = acc32 + TILE3;
   const int t = blockIdx.x;
   const int tz = t % g.nt, ty = (t / g.nt) % g.nt, tx = t / (g.nt * g.nt);
   const int x0 = tx * g.tdim, y0 = ty * g.tdim, z0 = tz * g.tdim;
   const int ex = min(g.tdim, g.N - x0), ey = min(g.tdim, g.N - y0), ez = min(g.tdim, g.N - z0);
 
-  {
-    longlong2* a2 = reinterpret_cast<longlong2*>(acc);
-    for (int k = threadIdx.x; k < G * TILE3 / 2; k += DEP_THREADS) a2[k] = make_longlong2(0, 0);
-  }
-  const int s = fixed_scale_exp(g.n, ctr->maxw_bits, CM);
-  const float sc = ldexpf(1.0f, s);
-  const float inv_sc = ldexpf(1.0f, -s);
-  __syncthreads();
-
   const unsigned end = cursors[t];
   const unsigned beg = end - counts[t];
-  for (unsigned i = beg + threadIdx.x; i < end; i += DEP_THREADS) {
-    const float4 e = entries[i];
-#pragma unroll
-    for (int grid = 0; grid < G; ++grid) {
+  const int s = fixed_scale_exp(ctr->maxw_bits, CM);
+  const float sc = ldexpf(1.0f, s);
+  const float inv_sc = ldexpf(1.0f, -s);
+  const long long N = g.N;
+  const long long M = N * N * N;
+  const bool vec4 = g.vec_ok && (ez == TILE) && ((g.N & 3) == 0);
+
+  for (int grid = 0; grid < G; ++grid) {
+    {
+      uint4* a4 = reinterpret_cast<uint4*>(acc32);
+      for (int k = threadIdx.x; k < 2 * TILE3 / 4; k += DEP_THREADS) a4[k] = make_uint4(0u, 0u, 0u, 0u);
+    }
+    __syncthreads();
+    for (unsigned i = beg + threadIdx.x; i < end; i += DEP_THREADS) {
+      const float4 e = entries[i];
       Axis<R> ax, ay, az;
       make_axis<MAS, CM>(g, e.x, grid, ax);
       make_axis<MAS, CM>(g, e.y, grid, ay);
@@ -358,7 +406,6 @@ deposit_kernel(DepGeom g, const float4* __restrict__ entries, const unsigned* __
       local_nodes<R>(ax, g.N, x0, ex, lx);
       local_nodes<R>(ay, g.N, y0, ey, ly);
       local_nodes<R>(az, g.N, z0, ez, lz);
-      unsigned long long* a = reinterpret_cast<unsigned long long*>(acc + grid * TILE3);
 #pragma unroll
       for (int rx = 0; rx < R; ++rx) {
         if (lx[rx] < 0) continue;
@@ -366,41 +413,49 @@ deposit_kernel(DepGeom g, const float4* __restrict__ entries, const unsigned* __
         for (int ry = 0; ry < R; ++ry) {
           if (ly[ry] < 0) continue;
           // src/mas.py:149 (and :76) weights corner (ix, iyp, izp) with
-          // mdx*mdy*ddz; the compat variants keep that (ryw below).
+          // mdx*mdy*ddz; the compat variants keep that (wxy_bug).  The
+          // product order ((wx*wy)*wz)*w is the reference's.
           const float wxy = __fmul_rn(ax.w[rx], ay.w[ry]);
           const float wxy_bug = __fmul_rn(ax.w[rx], ay.w[0]);
           const int row = (lx[rx] * TILE + ly[ry]) * TILE;
+          int q[R];
+          unsigned old[R];
 #pragma unroll
-          for (int rz = 0; rz < R; ++rz) {
+          for (int rz = 0; rz < R; ++rz) {         // issue the row's low-word adds together
             if (lz[rz] < 0) continue;
             const bool bug = CM != 0 && rx == 0 && ry == 1 && rz == 1;
             const float c = __fmul_rn(__fmul_rn(bug ? wxy_bug : wxy, az.w[rz]), e.w);
-            const long long q = __float2ll_rn(__fmul_rn(c, sc));
-            atomicAdd(&a[row + lz[rz]], static_cast<unsigned long long>(q));
+            q[rz] = __float2int_rn(__fmul_rn(c, sc));
+            old[rz] = atomicAdd(&lo[row + lz[rz]], static_cast<unsigned>(q[rz]));
+          }
+#pragma unroll
+          for (int rz = 0; rz < R; ++rz) {         // then the carries into the high words
+            if (lz[rz] < 0) continue;
+            const unsigned add = static_cast<unsigned>(q[rz]);
+            const int dh = (q[rz] < 0 ? -1 : 0) + (old[rz] + add < old[rz] ? 1 : 0);
+            if (dh) atomicAdd(&hi[row + lz[rz]], static_cast<unsigned>(dh));
           }
         }
       }
     }
-  }
-  __syncthreads();
+    __syncthreads();
 
-  // Write the tile once; sum it exactly for the mean density.
-  const long long N = g.N;
-  const long long M = N * N * N;
-  const bool vec4 = g.vec_ok && (ez == TILE) && ((g.N & 3) == 0);
-#pragma unroll
-  for (int grid = 0; grid < G; ++grid) {
-    const long long* a = acc + grid * TILE3;
+    // Write this grid's tile once; sum it exactly for the mean density.
     long long part = 0;
     if (vec4) {
       for (int k = threadIdx.x; k < TILE3 / 4; k += DEP_THREADS) {
         const int lz = (k % (TILE / 4)) * 4, ly = (k / (TILE / 4)) % TILE, lx = k / (TILE * TILE / 4);
         if (lx >= ex || ly >= ey) continue;
-        const longlong2 q01 = reinterpret_cast<const longlong2*>(a)[(lx * TILE + ly) * (TILE / 2) + lz / 2];
-        const longlong2 q23 = reinterpret_cast<const longlong2*>(a)[(lx * TILE + ly) * (TILE / 2) + lz / 2 + 1];
-        part += q01.x + q01.y + q23.x + q23.y;
-        float4 v = make_float4(__fmul_rn(__ll2float_rn(q01.x), inv_sc), __fmul_rn(__ll2float_rn(q01.y), inv_sc),
-                               __fmul_rn(__ll2float_rn(q23.x), inv_sc), __fmul_rn(__ll2float_rn(q23.y), inv_sc));
+        const int c0 = (lx * TILE + ly) * TILE + lz;
+        const uint4 l4 = *reinterpret_cast<const uint4*>(lo + c0);
+        const uint4 h4 = *reinterpret_cast<const uint4*>(hi + c0);
+        const long long q0 = (long long)(((unsigned long long)h4.x << 32) | l4.x);
+        const long long q1 = (long long)(((unsigned long long)h4.y << 32) | l4.y);
+        const long long q2 = (long long)(((unsigned long long)h4.z << 32) | l4.z);
+        const long long q3 = (long long)(((unsigned long long)h4.w << 32) | l4.w);
+        part += q0 + q1 + q2 + q3;
+        float4 v = make_float4(fixed_to_float(q0, inv_sc), fixed_to_float(q1, inv_sc), fixed_to_float(q2, inv_sc),
+                               fixed_to_float(q3, inv_sc));
         const long long gi = grid * M + ((x0 + lx) * N + (y0 + ly)) * N + (z0 + lz);
         if (mesh_in) {
           const float4 b = *reinterpret_cast<const float4*>(mesh_in + gi);
@@ -412,10 +467,10 @@ deposit_kernel(DepGeom g, const float4* __restrict__ entries, const unsigned* __
       for (int k = threadIdx.x; k < TILE3; k += DEP_THREADS) {
         const int lz = k % TILE, ly = (k / TILE) % TILE, lx = k / (TILE * TILE);
         if (lx >= ex || ly >= ey || lz >= ez) continue;
-        const long long q = a[k];
+        const long long q = (long long)(((unsigned long long)hi[k] << 32) | lo[k]);
         part += q;
         const long long gi = grid * M + ((x0 + lx) * N + (y0 + ly)) * N + (z0 + lz);
-        float v = __fmul_rn(__ll2float_rn(q), inv_sc);
+        float v = fixed_to_float(q, inv_sc);
         if (mesh_in) v = __fadd_rn(mesh_in[gi], v);
         mesh_out[gi] = v;
       }
@@ -423,6 +478,7 @@ deposit_kernel(DepGeom g, const float4* __restrict__ entries, const unsigned* __
     for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
     if ((threadIdx.x & 31) == 0 && part != 0)
       atomicAdd(&ctr->mass_fixed[grid], static_cast<unsigned long long>(part));
+    __syncthreads();                            // the next grid reuses the accumulators
   }
 }
 
@@ -443,7 +499,7 @@ __global__ void stats_kernel(const DepCounters* ctr, const float4* block_stats, 
   if (threadIdx.x == 0) {
     ff ta{0.f, 0.f}, tb{0.f, 0.f};
     for (int k = 0; k < (int)(blockDim.x >> 5); ++k) { ta = ff_add(ta, s_a[k]); tb = ff_add(tb, s_b[k]); }
-    const int s = fixed_scale_exp(n, ctr->maxw_bits, compat);
+    const int s = fixed_scale_exp(ctr->maxw_bits, compat);
     const double inv = ldexp(1.0, -s);
     for (int grid = 0; grid < 2; ++grid)
       out->mass[grid] = grid < G ? (double)(long long)ctr->mass_fixed[grid] * inv : 0.0;
@@ -531,7 +587,7 @@ int run_scheme(const Launch& q) {
     scatter_kernel<MAS, G, CM><<<L.nblocks, CNT_THREADS, 0, q.stream>>>(q.g, q.cursors, q.entries);
     GBP_LAUNCH_CHECK();
   }
-  const size_t smem = (size_t)G * TILE3 * sizeof(long long);
+  const size_t smem = (size_t)2 * TILE3 * sizeof(unsigned);   // lo + hi words, one grid
   // more than 48 KB of dynamic shared memory needs the opt-in (cheap, per call)
   GBP_CUDA_TRY(cudaFuncSetAttribute(deposit_kernel<MAS, G, CM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)smem));

@@ -58,6 +58,7 @@ struct PowGeom {
   int zero_dc;              // density mesh: delta(k=0) = 0 exactly
   float2* part_ff;          // [C][NV][nbe]
   int warps;
+  int groups;               // work groups (g.warps chunks each), one partial per group
 };
 
 struct SmemPlan {
@@ -98,7 +99,7 @@ __device__ __forceinline__ Smem load_tables(const PowGeom& g, unsigned char* sme
   const int h = g.N / 2;
   for (int k = threadIdx.x; k <= h; k += blockDim.x) {
     const float r = g.inv_sinc2[k];
-    float c = INTER ? 0.25f : 1.0f;             // interlacing averages two grids: |(a+b)/2|^2
+    float c = 1.0f;
     for (int p = 0; p < g.mas_order; ++p) c *= r;  // sinc^(-2 mas_order)
     s.c2[k] = c;
     if (INTER) s.eph[k] = g.eph[k];
@@ -131,7 +132,8 @@ __device__ __forceinline__ Pencil pencil_of(const PowGeom& g, const Smem& s, int
   const int ax = kx < 0 ? -kx : kx, ay = ky < 0 ? -ky : ky;
   Pencil p;
   p.kp2 = kx * kx + ky * ky;
-  p.cxy = s.c2[ax] * s.c2[ay];
+  // an interlaced pair is averaged, |(a + b)/2|^2: the 1/4 rides on the pencil constant
+  p.cxy = s.c2[ax] * s.c2[ay] * (INTER ? 0.25f : 1.0f);
   p.pr = 1.0f;
   p.pi = 0.0f;
   if (INTER) {  // exp(i pi (kx+ky)/N) from the |k| table (conjugate for k < 0)
@@ -190,18 +192,25 @@ __device__ __forceinline__ void bin_add(float* wb, int nbe, int bin, const float
   for (int q = 0; q < NV; ++q) wb[q * nbe + bin] += v[q];
 }
 
+// Fold the warps' bins (in warp order, float-float) into the group's partial
+// and clear them for the next group.
 template <int NV>
-__device__ __forceinline__ void cta_fold(const PowGeom& g, const Smem& s) {
+__device__ __forceinline__ void cta_fold(const PowGeom& g, const Smem& s, int grp) {
   __syncthreads();
-  float2* pf = g.part_ff + (long long)blockIdx.x * NV * g.nbe;
+  float2* pf = g.part_ff + (long long)grp * NV * g.nbe;
   for (int b = threadIdx.x; b < g.nbe; b += blockDim.x) {
 #pragma unroll
     for (int q = 0; q < NV; ++q) {
       ff acc{0.f, 0.f};
-      for (int w = 0; w < g.warps; ++w) acc = ff_add_f(acc, s.wbase[(w * NV + q) * g.nbe + b]);
+      for (int w = 0; w < g.warps; ++w) {
+        float* p = &s.wbase[(w * NV + q) * g.nbe + b];
+        acc = ff_add_f(acc, *p);
+        *p = 0.0f;
+      }
       pf[q * g.nbe + b] = make_float2(acc.hi, acc.lo);
     }
   }
+  __syncthreads();
 }
 
 // ---------------------------------------------------------------------------
@@ -209,16 +218,8 @@ __device__ __forceinline__ void cta_fold(const PowGeom& g, const Smem& s) {
 // both grids' arrays are 16-byte aligned and every lane's 4 modes are either
 // all in range or all out) and a chunk that is a multiple of 128.
 template <int NV, bool INTER>
-__global__ void __launch_bounds__(POW_WARPS * 32)
-power_kernel4(PowGeom g) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const Smem s = load_tables<NV, INTER>(g, smem);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  float* wb = s.wbase + warp * NV * g.nbe;
-  const long long wglob = (long long)blockIdx.x * g.warps + warp;
-  const long long beg = wglob * g.chunk;
-  const long long end = min(beg + g.chunk, g.total);
-
+__device__ __forceinline__ void chunk4(const PowGeom& g, const Smem& s, float* wb, int lane, long long beg,
+                                       long long end) {
   if (beg < end) {
     // first mode of this lane in the current step, and its pencil / kz
     long long f = beg + 4 * lane;
@@ -335,21 +336,13 @@ power_kernel4(PowGeom g) {
       }
     }
   }
-  cta_fold<NV>(g, s);
 }
 
 // ---------------------------------------------------------------------------
-// Simple kernel: one mode per lane per step (any N, any alignment).
+// Simple path: one mode per lane per step (any N, any alignment).
 template <int NV, bool INTER>
-__global__ void __launch_bounds__(POW_WARPS * 32)
-power_kernel1(PowGeom g) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const Smem s = load_tables<NV, INTER>(g, smem);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  float* wb = s.wbase + warp * NV * g.nbe;
-  const long long wglob = (long long)blockIdx.x * g.warps + warp;
-  const long long beg = wglob * g.chunk;
-  const long long end = min(beg + g.chunk, g.total);
+__device__ __forceinline__ void chunk1(const PowGeom& g, const Smem& s, float* wb, int lane, long long beg,
+                                       long long end) {
   if (beg < end) {
     long long f = beg + lane;
     long long pen = f / g.Lz;
@@ -376,7 +369,7 @@ power_kernel1(PowGeom g) {
       const bool segend = (lane == 31) || ((heads >> (lane + 1)) & 1u);
       const int pid = ix * g.N + iy;
       const int rel = pid - __shfl_sync(0xffffffffu, pid, 0);
-      const int nph = __shfl_sync(0xffffffffu, rel, 31) + 1;
+      const int nph = __reduce_max_sync(0xffffffffu, valid ? rel : 0) + 1;   // pencils in this step
       for (int ph = 0; ph < nph; ++ph) {
         if (segend && bin >= 0 && rel == ph) bin_add<NV>(wb, g.nbe, bin, v);
         __syncwarp();
@@ -389,7 +382,25 @@ power_kernel1(PowGeom g) {
       }
     }
   }
-  cta_fold<NV>(g, s);
+}
+
+// Persistent CTAs walk the fixed work groups (g.warps warp chunks each); a
+// group's sums go to its own partial, so the result does not depend on how
+// many CTAs run.
+template <int NV, bool INTER, bool WIDE>
+__global__ void __launch_bounds__(POW_WARPS * 32, 4)
+power_kernel(PowGeom g) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const Smem s = load_tables<NV, INTER>(g, smem);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float* wb = s.wbase + warp * NV * g.nbe;
+  for (int grp = blockIdx.x; grp < g.groups; grp += gridDim.x) {
+    const long long beg = ((long long)grp * g.warps + warp) * g.chunk;
+    const long long end = min(beg + g.chunk, g.total);
+    if (WIDE) chunk4<NV, INTER>(g, s, wb, lane, beg, end);
+    else chunk1<NV, INTER>(g, s, wb, lane, beg, end);
+    cta_fold<NV>(g, s, grp);
+  }
 }
 
 // One warp per bin: fold the CTA partials (fixed order) into double moment
@@ -464,7 +475,7 @@ int power_layout(const gbp_bins_s* B, int G, int ells, PowLayout& L) {
   L.warps = w;
   L.total = (long long)B->N * B->N * (B->N / 2 + 1);
   L.wide = (B->N % 2 == 0) && B->N >= 64;
-  long long target = L.total / (8LL * 152 * 4);
+  long long target = L.total / (8LL * 152 * 8);   // ~8 groups per SM on a GB300
   target = std::max(1024LL, std::min(16384LL, target));
   L.chunk = (target + 127) & ~127LL;
   const long long nw = (L.total + L.chunk - 1) / L.chunk;
@@ -531,13 +542,20 @@ extern "C" int gbp_power(const void* spectrum, int G, gbp_bins B, int mas_order,
 
   void (*kern)(PowGeom) = nullptr;
   const bool inter = G == 2;
-#define GBP_PICK(NVv)                                                                               \
-  kern = wide ? (inter ? power_kernel4<NVv, true> : power_kernel4<NVv, false>)                   \
-              : (inter ? power_kernel1<NVv, true> : power_kernel1<NVv, false>);
+#define GBP_PICK(NVv)                                                                                   \
+  kern = wide ? (inter ? power_kernel<NVv, true, true> : power_kernel<NVv, false, true>)               \
+              : (inter ? power_kernel<NVv, true, false> : power_kernel<NVv, false, false>);
   if (L.NV == 1) { GBP_PICK(1) } else if (L.NV == 2) { GBP_PICK(2) } else { GBP_PICK(3) }
 #undef GBP_PICK
   GBP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem));
-  kern<<<L.C, L.warps * 32, L.smem, stream>>>(g);
+  // persistent grid: as many CTAs as fit on the device at once (never more than the groups)
+  int dev = 0, sms = 0, per_sm = 0;
+  GBP_CUDA_TRY(cudaGetDevice(&dev));
+  GBP_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  GBP_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, L.warps * 32, L.smem));
+  g.groups = L.C;
+  const int grid = std::max(1, std::min(L.C, sms * std::max(per_sm, 1)));
+  kern<<<grid, L.warps * 32, L.smem, stream>>>(g);
   GBP_LAUNCH_CHECK();
   const int wpb = 8;
   power_reduce_kernel<<<(B->nb + wpb - 1) / wpb, wpb * 32, 0, stream>>>(

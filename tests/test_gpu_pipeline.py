@@ -30,8 +30,9 @@ def _check(res, ref, kmean=True):
     np.testing.assert_array_equal(nm, ref["nmodes"])
     full = nm > 0
     pk = res.pk.cpu().numpy()
-    amp = np.abs(ref["pk"][full, 0] + ref.get("shot", 0.0))
-    amp = np.maximum(amp, 1e-9 * amp.max())     # a bin holding only k=0 has zero power
+    # scale of the two terms of P_0 = raw - shot (a bin holding only k=0 has raw == 0)
+    amp = np.abs(ref["pk"][full, 0] + ref.get("shot", 0.0)) + ref.get("shot", 0.0)
+    amp = np.maximum(amp, 1e-9 * amp.max())
     for l in (0, 1, 2):
         err = np.abs(pk[full, l] - ref["pk"][full, l])
         assert np.all(err <= RTOL_P * amp), (l, (err / amp).max())
@@ -93,7 +94,7 @@ def test_shot_noise_and_mass_bookkeeping():
     b = no_sn.run(*t).pk.cpu().numpy()
     st = read_stats(with_sn.stats)
     w64 = w.astype(np.float64)
-    np.testing.assert_allclose(st.mass[0], w64.sum(), rtol=1e-12)
+    np.testing.assert_allclose(st.mass[0], w64.sum(), rtol=1e-9)   # exact sum of 2^-s-quantised terms
     np.testing.assert_allclose(st.sum_w, w64.sum(), rtol=1e-7)
     np.testing.assert_allclose(st.sum_w2, (w64 * w64).sum(), rtol=1e-7)
     assert st.n_kept == x.size and st.n_nonfinite == 0
