@@ -244,7 +244,8 @@ def main():
         ev[1].record(stream)
         ps.plan.execute(ps.mesh, ps.spec, ps.fft_ws)
         ev[2].record(stream)
-        _native.power(ps.spec, G, ps.bins, mas_order=cfg.mas_order, ells=ps.ells, mass=ps.stats, ws=ps.pow_ws,
+        _native.power(ps.spec, G, ps.bins, mas_order=cfg.mas_order, ells=ps.ells, z_pitch=ps.plan.pitch,
+                      mass=ps.stats, ws=ps.pow_ws,
                       out=ps.sums)
         ev[3].record(stream)
         _native.normalize(ps.sums, n_mesh=N, box_size=cfg.box_size, mass=ps.stats, stats=ps.stats,

@@ -16,8 +16,8 @@
  *     Interlaced deposits write two meshes back to back: grid 0 at mesh_out,
  *     grid 1 (particles shifted by +half a cell on every axis) at
  *     mesh_out + n_mesh^3.
- *   - Spectra are complex64 [x][y][z] with n_mesh/2+1 entries along z (the
- *     cuFFT real-to-complex layout), one per grid, back to back.
+ *   - Spectra are complex64 [x][y][z]: n_mesh/2+1 modes along z in rows of
+ *     z_pitch entries (see gbp_fft_plan_pitch), one grid after the other.
  *   - Results are deterministic: the same inputs give bitwise-identical
  *     outputs on every run, whatever else shares the GPU.
  */
@@ -103,14 +103,20 @@ int gbp_deposit(const float* x, const float* y, const float* z, const float* w,
                 size_t workspace_bytes, gbp_stream_t stream);
 
 /* ------------------------------------------------------------------------
- * FFT plans: a cached cuFFT 3D real-to-complex plan for n_grids meshes of
- * side n_mesh.  Replaces the jnp.fft.rfftn of src/correlations.py:22.
- * The plan does not own a work area; gbp_fft_r2c takes one.
+ * FFT plans: 3-D real-to-complex transform of n_grids meshes of side n_mesh
+ * (forward, unnormalised, as jnp.fft.rfftn).  Replaces the rfftn of
+ * src/correlations.py:22.  Power-of-two meshes 64..1024 use the library's
+ * own three-pass transform; other sizes a cuFFT plan.  The spectrum rows are
+ * z_pitch complex apart (gbp_fft_plan_pitch: n/2+8 for the library's
+ * transform, n/2+1 for cuFFT), the first n/2+1 of each row being the modes.
+ * A cuFFT plan needs a work area (workspace_bytes); the library's needs none.
+ * Buffers passed to gbp_fft_r2c must be 16-byte aligned.
  * ---------------------------------------------------------------------- */
 typedef struct gbp_fft_plan_s* gbp_fft_plan;
 
 int gbp_fft_plan_create(int n_mesh, int n_grids, gbp_fft_plan* plan,
                         size_t* workspace_bytes);
+int gbp_fft_plan_pitch(gbp_fft_plan plan, int* z_pitch);
 int gbp_fft_plan_destroy(gbp_fft_plan plan);
 int gbp_fft_r2c(gbp_fft_plan plan, const float* mesh, void* spectrum,
                 void* workspace, size_t workspace_bytes, gbp_stream_t stream);
@@ -150,7 +156,9 @@ int gbp_bins_info(gbp_bins bins, int* n_bins, int* n_reach,
  * |delta_k|^2 x L_l(mu) (line of sight = z) and k-shell binning.
  * Replaces src/correlations.py:20-48 (the body of powspec_vec).
  *
- *   spectrum     complex64 [n_grids][n_mesh][n_mesh][n_mesh/2+1].
+ *   spectrum     complex64 [n_grids][n_mesh][n_mesh][z_pitch]; the first
+ *                n_mesh/2+1 entries of each z row are the modes.
+ *   z_pitch      complex entries per z row (>= n_mesh/2+1; 0 means n_mesh/2+1).
  *   n_grids      1, or 2 for an interlaced pair: the modes are combined as
  *                (F0 + F1 exp(i pi (kx+ky+kz)/n_mesh)) / 2.
  *   mas_order    window: each axis is divided by sinc(pi k_i/n)^mas_order
@@ -166,11 +174,11 @@ int gbp_bins_info(gbp_bins bins, int* n_bins, int* n_reach,
  *                src/correlations.py:48 counts them).
  *   ksum_out     double[n_bins] sum of |k| in grid units (GBP_KSUM), or NULL.
  * ---------------------------------------------------------------------- */
-int gbp_power_workspace_size(gbp_bins bins, int n_grids, int ells,
+int gbp_power_workspace_size(gbp_bins bins, int n_grids, int z_pitch, int ells,
                              size_t* bytes);
 
-int gbp_power(const void* spectrum, int n_grids, gbp_bins bins, int mas_order,
-              int ells, const double* mass, double* sums_out,
+int gbp_power(const void* spectrum, int n_grids, int z_pitch, gbp_bins bins,
+              int mas_order, int ells, const double* mass, double* sums_out,
               long long* nmodes_out, double* ksum_out, void* workspace,
               size_t workspace_bytes, gbp_stream_t stream);
 

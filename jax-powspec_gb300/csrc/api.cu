@@ -203,16 +203,44 @@ extern "C" int gbp_bins_info(gbp_bins B, int* nb, int* reach, int32_t* last) {
 }
 
 // ---------------------------------------------------------------------------
-// cuFFT plan: 3D R2C, batch = number of grids, caller-provided work area.
+// FFT plans.  Power-of-two meshes 64..1024 use the library's own three-pass
+// transform (fft.cu), which writes z rows padded to N/2+8 complex; other
+// sizes use a cuFFT 3-D R2C plan (batch = grids) with unpadded rows of
+// N/2+1.  Setting GBP_FFT_BACKEND=cufft when the plan is created forces
+// cuFFT (used to cross-check the two).
+namespace gbp {
+bool own_fft_supported(int N);
+int own_fft_pitch(int N);
+int own_fft_twiddles(int N, float2** d_tw);
+int own_fft_r2c(int N, int G, const float* mesh, float2* spec, const float2* tw, cudaStream_t st);
+}  // namespace gbp
+
 struct gbp_fft_plan_s {
+  bool own;
   cufftHandle h;
-  int n, grids;
+  float2* tw;       // own transform: twiddles exp(-2 pi i e / N)
+  int n, grids, pitch;
   size_t ws;
 };
 
 extern "C" int gbp_fft_plan_create(int n, int grids, gbp_fft_plan* out, size_t* ws_bytes) {
   if (!out || n < 2 || n > 4096 || grids < 1 || grids > 64) return GBP_ERR_INVALID;
   *out = nullptr;
+  const char* env = getenv("GBP_FFT_BACKEND");
+  const bool force_cufft = env && strcmp(env, "cufft") == 0;
+  if (own_fft_supported(n) && !force_cufft) {
+    float2* tw = nullptr;
+    const int st = own_fft_twiddles(n, &tw);
+    if (st) return st;
+    gbp_fft_plan_s* p = new (std::nothrow) gbp_fft_plan_s{true, 0, tw, n, grids, own_fft_pitch(n), 0};
+    if (!p) {
+      cudaFree(tw);
+      return GBP_ERR_ALLOC;
+    }
+    *out = p;
+    if (ws_bytes) *ws_bytes = 0;
+    return GBP_OK;
+  }
   cufftHandle h;
   if (cufftCreate(&h) != CUFFT_SUCCESS) return GBP_ERR_CUFFT;
   if (cufftSetAutoAllocation(h, 0) != CUFFT_SUCCESS) {
@@ -227,7 +255,7 @@ extern "C" int gbp_fft_plan_create(int n, int grids, gbp_fft_plan* out, size_t* 
     cufftDestroy(h);
     return GBP_ERR_CUFFT;
   }
-  gbp_fft_plan_s* p = new (std::nothrow) gbp_fft_plan_s{h, n, grids, ws};
+  gbp_fft_plan_s* p = new (std::nothrow) gbp_fft_plan_s{false, h, nullptr, n, grids, n / 2 + 1, ws};
   if (!p) {
     cufftDestroy(h);
     return GBP_ERR_ALLOC;
@@ -237,9 +265,16 @@ extern "C" int gbp_fft_plan_create(int n, int grids, gbp_fft_plan* out, size_t* 
   return GBP_OK;
 }
 
+extern "C" int gbp_fft_plan_pitch(gbp_fft_plan p, int* z_pitch) {
+  if (!p || !z_pitch) return GBP_ERR_INVALID;
+  *z_pitch = p->pitch;
+  return GBP_OK;
+}
+
 extern "C" int gbp_fft_plan_destroy(gbp_fft_plan p) {
   if (!p) return GBP_ERR_INVALID;
-  cufftDestroy(p->h);
+  if (p->own) cudaFree(p->tw);
+  else cufftDestroy(p->h);
   delete p;
   return GBP_OK;
 }
@@ -247,6 +282,12 @@ extern "C" int gbp_fft_plan_destroy(gbp_fft_plan p) {
 extern "C" int gbp_fft_r2c(gbp_fft_plan p, const float* mesh, void* spec, void* ws, size_t ws_bytes,
                            gbp_stream_t stream) {
   if (!p || !mesh || !spec) return GBP_ERR_INVALID;
+  if (p->own) {
+    // float4 loads and stores: both buffers must be 16-byte aligned
+    if (((reinterpret_cast<uintptr_t>(mesh) | reinterpret_cast<uintptr_t>(spec)) & 15u) != 0) return GBP_ERR_INVALID;
+    return own_fft_r2c(p->n, p->grids, mesh, static_cast<float2*>(spec), p->tw,
+                       reinterpret_cast<cudaStream_t>(stream));
+  }
   if (p->ws > 0 && (!ws || ws_bytes < p->ws)) return GBP_ERR_WORKSPACE;
   if (cufftSetStream(p->h, reinterpret_cast<cudaStream_t>(stream)) != CUFFT_SUCCESS) return GBP_ERR_CUFFT;
   if (p->ws > 0 && cufftSetWorkArea(p->h, ws) != CUFFT_SUCCESS) return GBP_ERR_CUFFT;

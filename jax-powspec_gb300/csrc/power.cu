@@ -44,7 +44,8 @@ constexpr int POW_WARPS = 8;
 struct PowGeom {
   const float2* s0;
   const float2* s1;
-  int N, Lz;
+  int N, Lz;                // Lz = N/2+1 modes per z row
+  int Lzs;                  // z row pitch (>= Lz); entries kz >= Lz are padding
   long long total;          // N*N*Lz modes per grid
   long long chunk;          // modes per warp
   int nb, nbe;              // bins, bins some mode can reach
@@ -223,8 +224,8 @@ __device__ __forceinline__ void chunk4(const PowGeom& g, const Smem& s, float* w
   if (beg < end) {
     // first mode of this lane in the current step, and its pencil / kz
     long long f = beg + 4 * lane;
-    long long pen = f / g.Lz;
-    int kz = (int)(f - pen * g.Lz);
+    long long pen = f / g.Lzs;
+    int kz = (int)(f - pen * g.Lzs);
     int iy = (int)(pen % g.N);
     int ix = (int)(pen / g.N);
     const float4* s0 = reinterpret_cast<const float4*>(g.s0);
@@ -258,7 +259,7 @@ __device__ __forceinline__ void chunk4(const PowGeom& g, const Smem& s, float* w
         Pencil pc = pencil_of<INTER>(g, s, cix, ciy);
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-          if (j > 0 && ++ckz == g.Lz) {
+          if (j > 0 && ++ckz == g.Lzs) {
             ckz = 0;
             if (++ciy == g.N) { ciy = 0; ++cix; }
             pc = pencil_of<INTER>(g, s, cix, ciy);
@@ -266,8 +267,9 @@ __device__ __forceinline__ void chunk4(const PowGeom& g, const Smem& s, float* w
           pid[j] = cix * g.N + ciy;
           int k2;
           const bool zero = g.zero_dc && (f + j == 0);
-          mode_moments<NV, INTER>(s, pc, ckz, A[j], Bv[j], zero, P[j], k2);
-          bin[j] = valid ? bin_of(g, s, k2) : -1;
+          const bool real_mode = ckz < g.Lz;     // not row padding
+          mode_moments<NV, INTER>(s, pc, real_mode ? ckz : 0, A[j], Bv[j], zero || !real_mode, P[j], k2);
+          bin[j] = (valid && real_mode) ? bin_of(g, s, k2) : -1;
         }
       }
       // in-lane runs: P[j] becomes the sum of the run up to mode j
@@ -330,8 +332,8 @@ __device__ __forceinline__ void chunk4(const PowGeom& g, const Smem& s, float* w
       a01 = na01; a23 = na23; b01 = nb01; b23 = nb23;
       f += 128;
       kz += 128;
-      while (kz >= g.Lz) {
-        kz -= g.Lz;
+      while (kz >= g.Lzs) {
+        kz -= g.Lzs;
         if (++iy == g.N) { iy = 0; ++ix; }
       }
     }
@@ -345,8 +347,8 @@ __device__ __forceinline__ void chunk1(const PowGeom& g, const Smem& s, float* w
                                        long long end) {
   if (beg < end) {
     long long f = beg + lane;
-    long long pen = f / g.Lz;
-    int kz = (int)(f - pen * g.Lz);
+    long long pen = f / g.Lzs;
+    int kz = (int)(f - pen * g.Lzs);
     int iy = (int)(pen % g.N);
     int ix = (int)(pen / g.N);
     for (long long fb = beg; fb < end; fb += 32) {
@@ -355,7 +357,7 @@ __device__ __forceinline__ void chunk1(const PowGeom& g, const Smem& s, float* w
 #pragma unroll
       for (int q = 0; q < NV; ++q) v[q] = 0.0f;
       int bin = -1;
-      if (valid) {
+      if (valid && kz < g.Lz) {
         const Pencil pc = pencil_of<INTER>(g, s, ix, iy);
         const float2 a = g.s0[f];
         const float2 b = INTER ? g.s1[f] : make_float2(0.f, 0.f);
@@ -376,8 +378,8 @@ __device__ __forceinline__ void chunk1(const PowGeom& g, const Smem& s, float* w
       }
       f += 32;
       kz += 32;
-      while (kz >= g.Lz) {
-        kz -= g.Lz;
+      while (kz >= g.Lzs) {
+        kz -= g.Lzs;
         if (++iy == g.N) { iy = 0; ++ix; }
       }
     }
@@ -465,7 +467,8 @@ struct PowLayout {
 
 // A pure function of (N, bins, ells): the summation order, and therefore the
 // result, is the same on every device.
-int power_layout(const gbp_bins_s* B, int G, int ells, PowLayout& L) {
+int power_layout(const gbp_bins_s* B, int G, int ells, int Lzs, PowLayout& L) {
+  if (Lzs < B->N / 2 + 1) return GBP_ERR_INVALID;
   L.NV = (ells & GBP_ELL4) ? 3 : ((ells & GBP_ELL2) ? 2 : 1);
   const size_t budget = 200 * 1024;
   int w = POW_WARPS;
@@ -473,8 +476,8 @@ int power_layout(const gbp_bins_s* B, int G, int ells, PowLayout& L) {
   L.smem = smem_plan(B->N, B->nbe, B->lut_n, w, L.NV).total;
   if (L.smem > budget) return GBP_ERR_UNSUPPORTED;
   L.warps = w;
-  L.total = (long long)B->N * B->N * (B->N / 2 + 1);
-  L.wide = (B->N % 2 == 0) && B->N >= 64;
+  L.total = (long long)B->N * B->N * Lzs;
+  L.wide = (B->N % 2 == 0) && B->N >= 64;   // N*N*Lzs stays a multiple of 4 modes
   long long target = L.total / (8LL * 152 * 8);   // ~8 groups per SM on a GB300
   target = std::max(1024LL, std::min(16384LL, target));
   L.chunk = (target + 127) & ~127LL;
@@ -490,26 +493,27 @@ int power_layout(const gbp_bins_s* B, int G, int ells, PowLayout& L) {
 
 using namespace gbp;
 
-extern "C" int gbp_power_workspace_size(gbp_bins bins, int G, int ells, size_t* bytes) {
+extern "C" int gbp_power_workspace_size(gbp_bins bins, int G, int z_pitch, int ells, size_t* bytes) {
   if (!bins || !bytes || (G != 1 && G != 2)) return GBP_ERR_INVALID;
   PowLayout L;
-  const int st = power_layout(bins, G, ells, L);
+  const int st = power_layout(bins, G, ells, z_pitch > 0 ? z_pitch : bins->N / 2 + 1, L);
   if (st) return st;
   *bytes = L.ws_total;
   return GBP_OK;
 }
 
-extern "C" int gbp_power(const void* spectrum, int G, gbp_bins B, int mas_order, int ells, const double* mass,
-                         double* sums_out, long long* nmodes_out, double* ksum_out, void* workspace,
-                         size_t ws_bytes, gbp_stream_t stream_) {
+extern "C" int gbp_power(const void* spectrum, int G, int z_pitch, gbp_bins B, int mas_order, int ells,
+                         const double* mass, double* sums_out, long long* nmodes_out, double* ksum_out,
+                         void* workspace, size_t ws_bytes, gbp_stream_t stream_) {
   cudaStream_t stream = reinterpret_cast<cudaStream_t>(stream_);
   if (!spectrum || !B || !sums_out || !nmodes_out) return GBP_ERR_INVALID;
   if (G != 1 && G != 2) return GBP_ERR_INVALID;
   if (mas_order < 0 || mas_order > 8) return GBP_ERR_INVALID;
   if ((ells & (GBP_ELL0 | GBP_ELL2 | GBP_ELL4)) == 0 || (ells & ~15)) return GBP_ERR_INVALID;
   if ((ells & GBP_KSUM) && !ksum_out) return GBP_ERR_INVALID;
+  const int Lzs = z_pitch > 0 ? z_pitch : B->N / 2 + 1;
   PowLayout L;
-  int st = power_layout(B, G, ells, L);
+  int st = power_layout(B, G, ells, Lzs, L);
   if (st) return st;
   if (!workspace || ws_bytes < L.ws_total) return GBP_ERR_WORKSPACE;
 
@@ -521,6 +525,7 @@ extern "C" int gbp_power(const void* spectrum, int G, gbp_bins B, int mas_order,
   g.s1 = G == 2 ? g.s0 + L.total : nullptr;
   g.N = B->N;
   g.Lz = B->N / 2 + 1;
+  g.Lzs = Lzs;
   g.total = L.total;
   g.chunk = L.chunk;
   g.nb = B->nb;

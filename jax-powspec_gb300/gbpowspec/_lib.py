@@ -57,14 +57,15 @@ SIGNATURES = [
     ("gbp_deposit", _i, [_vp, _vp, _vp, _vp, _i64, _f, _f, _f, _f, _i, _i, _i, _i, _i,
                          _vp, _vp, _vp, _vp, _sz, _vp]),
     ("gbp_fft_plan_create", _i, [_i, _i, C.POINTER(_vp), C.POINTER(_sz)]),
+    ("gbp_fft_plan_pitch", _i, [_vp, C.POINTER(_i)]),
     ("gbp_fft_plan_destroy", _i, [_vp]),
     ("gbp_fft_r2c", _i, [_vp, _vp, _vp, _vp, _sz, _vp]),
     ("gbp_bin_thresholds", _i, [_vp, _i, _i, _vp, C.POINTER(C.c_int32), C.POINTER(_i)]),
     ("gbp_bins_create", _i, [_vp, _i, _i, C.POINTER(_vp)]),
     ("gbp_bins_destroy", _i, [_vp]),
     ("gbp_bins_info", _i, [_vp, C.POINTER(_i), C.POINTER(_i), C.POINTER(C.c_int32)]),
-    ("gbp_power_workspace_size", _i, [_vp, _i, _i, C.POINTER(_sz)]),
-    ("gbp_power", _i, [_vp, _i, _vp, _i, _i, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
+    ("gbp_power_workspace_size", _i, [_vp, _i, _i, _i, C.POINTER(_sz)]),
+    ("gbp_power", _i, [_vp, _i, _i, _vp, _i, _i, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     ("gbp_power_normalize", _i, [_vp, _vp, _vp, _i, _i, _d, _vp, _vp, _i, _vp, _vp, _vp]),
 ]
 

@@ -102,22 +102,33 @@ def deposit(x: torch.Tensor, y: torch.Tensor, z: torch.Tensor, w: torch.Tensor |
 
 # ---------------------------------------------------------------- FFT plans
 class FFTPlan:
-    """cuFFT R2C plan for `grids` meshes of side n (owned; freed on close)."""
+    """3-D R2C plan for `grids` meshes of side n (owned; freed on close).
+
+    `pitch` is the number of complex entries per z row of the spectrum it
+    writes (the first n//2+1 are the modes); `spectrum_floats` the float32
+    count of a buffer that holds all grids' spectra.
+    """
 
     def __init__(self, n: int, grids: int, device: torch.device):
         lib = _lib.load()
         self.n, self.grids, self.device = int(n), int(grids), device
         h = C.c_void_p()
         wsb = C.c_size_t(0)
+        pitch = C.c_int(0)
         with torch.cuda.device(device):
             check(lib.gbp_fft_plan_create(self.n, self.grids, C.byref(h), C.byref(wsb)), "gbp_fft_plan_create")
-        self.handle, self.ws_bytes = h, wsb.value
+            check(lib.gbp_fft_plan_pitch(h, C.byref(pitch)), "gbp_fft_plan_pitch")
+        self.handle, self.ws_bytes, self.pitch = h, wsb.value, pitch.value
+
+    @property
+    def spectrum_floats(self) -> int:
+        return self.grids * self.n * self.n * self.pitch * 2
 
     def execute(self, mesh: torch.Tensor, spec: torch.Tensor, ws: torch.Tensor | None = None) -> torch.Tensor:
         n, G = self.n, self.grids
         if mesh.numel() != G * n ** 3 or mesh.dtype != _F32 or not mesh.is_contiguous():
             raise ValueError("mesh does not match the plan")
-        if spec.numel() * spec.element_size() < G * n * n * (n // 2 + 1) * 8:
+        if spec.numel() * spec.element_size() < self.spectrum_floats * 4:
             raise ValueError("spectrum buffer too small")
         if self.ws_bytes and (ws is None or ws.numel() < self.ws_bytes):
             ws = workspace(self.ws_bytes, mesh.device)
@@ -211,27 +222,28 @@ class PowerSums:
     ksum: torch.Tensor | None
 
 
-def power_workspace_size(bins: Bins, grids: int, ells: int) -> int:
+def power_workspace_size(bins: Bins, grids: int, ells: int, z_pitch: int = 0) -> int:
     out = C.c_size_t(0)
-    check(_lib.load().gbp_power_workspace_size(bins.handle, int(grids), int(ells), C.byref(out)),
+    check(_lib.load().gbp_power_workspace_size(bins.handle, int(grids), int(z_pitch), int(ells), C.byref(out)),
           "gbp_power_workspace_size")
     return out.value
 
 
-def power(spec: torch.Tensor, grids: int, bins: Bins, *, mas_order: int, ells: int,
+def power(spec: torch.Tensor, grids: int, bins: Bins, *, mas_order: int, ells: int, z_pitch: int = 0,
           mass: torch.Tensor | None = None, ws: torch.Tensor | None = None,
           out: PowerSums | None = None) -> PowerSums:
+    """Binned moments of a spectrum whose z rows are `z_pitch` complex apart (0: n//2+1)."""
     dev = spec.device
     nb = bins.n_bins
     if out is None:
         out = PowerSums(torch.empty((nb, 3), dtype=torch.float64, device=dev),
                         torch.empty(nb, dtype=torch.int64, device=dev),
                         torch.empty(nb, dtype=torch.float64, device=dev) if ells & _lib.KSUM else None)
-    need = power_workspace_size(bins, grids, ells)
+    need = power_workspace_size(bins, grids, ells, z_pitch)
     if ws is None or ws.numel() < need:
         ws = workspace(need, dev)
-    check(_lib.load().gbp_power(_ptr(spec), int(grids), bins.handle, int(mas_order), int(ells), _ptr(mass),
-                                _ptr(out.sums), _ptr(out.nmodes), _ptr(out.ksum), _ptr(ws), ws.numel(),
+    check(_lib.load().gbp_power(_ptr(spec), int(grids), int(z_pitch), bins.handle, int(mas_order), int(ells),
+                                _ptr(mass), _ptr(out.sums), _ptr(out.nmodes), _ptr(out.ksum), _ptr(ws), ws.numel(),
                                 _stream_of(dev)), "gbp_power")
     return out
 

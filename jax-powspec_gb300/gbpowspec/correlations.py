@@ -63,9 +63,9 @@ def _binned_power(d: torch.Tensor, kedges_grid: np.ndarray, box: np.float32):
     dev = d.device
     bins = _native.bins_for(kedges_grid, N, dev)
     plan = _native.fft_plan(N, 1, dev)
-    spec = torch.empty(N * N * (N // 2 + 1) * 2, dtype=torch.float32, device=dev)
+    spec = torch.empty(plan.spectrum_floats, dtype=torch.float32, device=dev)
     plan.execute(d, spec)
-    ps = _native.power(spec, 1, bins, mas_order=2, ells=_lib.ELL0 | _lib.ELL2 | _lib.ELL4)
+    ps = _native.power(spec, 1, bins, mas_order=2, ells=_lib.ELL0 | _lib.ELL2 | _lib.ELL4, z_pitch=plan.pitch)
     pk, _ = _native.normalize(ps, n_mesh=N, box_size=float(box))
     return ps, pk
 

@@ -105,9 +105,9 @@ class PowerSpectrum:
         N, G = cfg.n_mesh, cfg.grids
         dev = self.device
         self.mesh = torch.empty((G, N, N, N), dtype=torch.float32, device=dev)
-        self.spec = torch.empty(G * N * N * (N // 2 + 1) * 2, dtype=torch.float32, device=dev)
         self.stats = torch.empty(_lib.STATS_BYTES, dtype=torch.uint8, device=dev)
         self.plan = _native.fft_plan(N, G, dev)
+        self.spec = torch.empty(self.plan.spectrum_floats, dtype=torch.float32, device=dev)
         self.fft_ws = _native.workspace(self.plan.ws_bytes, dev)
         self.bins = _native.bins_for(cfg.kedges_grid(), N, dev)
         self.ells = cfg.ells_mask()
@@ -117,7 +117,7 @@ class PowerSpectrum:
                                       torch.empty(nb, dtype=torch.float64, device=dev) if cfg.kmean else None)
         self.pk = torch.empty((nb, 3), dtype=torch.float64, device=dev)
         self.kmean = torch.empty(nb, dtype=torch.float64, device=dev) if cfg.kmean else None
-        self.pow_ws = _native.workspace(_native.power_workspace_size(self.bins, G, self.ells), dev)
+        self.pow_ws = _native.workspace(_native.power_workspace_size(self.bins, G, self.ells, self.plan.pitch), dev)
         self.dep_ws = None
         edges = cfg.edges()
         self.k_edges = edges
@@ -144,7 +144,8 @@ class PowerSpectrum:
                         out=self.mesh, stats=self.stats, ws=self._dep_ws(n))
         self.plan.execute(self.mesh, self.spec, self.fft_ws)
         mass = self.stats  # gbp_deposit_stats starts with double mass[2]
-        _native.power(self.spec, cfg.grids, self.bins, mas_order=cfg.mas_order, ells=self.ells, mass=mass,
+        _native.power(self.spec, cfg.grids, self.bins, mas_order=cfg.mas_order, ells=self.ells,
+                      z_pitch=self.plan.pitch, mass=mass,
                       ws=self.pow_ws, out=self.sums)
         _native.normalize(self.sums, n_mesh=N, box_size=cfg.box_size, mass=mass, stats=self.stats,
                           subtract_shot=cfg.shot_noise, pk_out=self.pk, kmean_out=self.kmean)
