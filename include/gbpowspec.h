@@ -183,6 +183,25 @@ int gbp_power(const void* spectrum, int n_grids, int z_pitch, gbp_bins bins,
               size_t workspace_bytes, gbp_stream_t stream);
 
 /* ------------------------------------------------------------------------
+ * gbp_power without a workspace argument: the same result, with its scratch
+ * held in a fixed 16 MiB device array inside the library, for callers that
+ * cannot allocate device memory when they call in (a JAX/XLA custom call gets
+ * only its operand and result buffers; a thread recording the stream into a
+ * CUDA graph may not cudaMalloc).  This entry point has no counterpart in the
+ * reference.
+ * Limit: (work groups) x (moments) x (bins) <= 2^21 float2, which holds any
+ * 512^3 mesh with up to ~560 bins of l = 0,2,4; larger requests return
+ * GBP_ERR_UNSUPPORTED without launching.  The first call on a device looks up
+ * the array's address with that device current: make it before any stream
+ * capture.  Calls share the array, so calls that overlap on the GPU race.
+ * ---------------------------------------------------------------------- */
+int gbp_power_noalloc(const void* spectrum, int n_grids, int z_pitch,
+                      gbp_bins bins, int mas_order, int ells,
+                      const double* mass, double* sums_out,
+                      long long* nmodes_out, double* ksum_out,
+                      gbp_stream_t stream);
+
+/* ------------------------------------------------------------------------
  * Normalisation of gbp_power's sums into P_l(k), on the device.
  * Replaces src/correlations.py:49-54 (and the caller-side shot-noise
  * subtraction of tests/correlations.py:36,83).

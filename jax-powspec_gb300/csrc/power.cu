@@ -32,6 +32,7 @@
 #include <math.h>
 
 #include <algorithm>
+#include <mutex>
 
 #include "gbp_bins.h"
 #include "gbp_internal.cuh"
@@ -581,6 +582,125 @@ extern "C" int gbp_power_normalize(const double* sums, const long long* nmodes, 
   const double kf = 2.0 * M_PI / box;
   power_normalize_kernel<<<(nb + 127) / 128, 128, 0, stream>>>(sums, nmodes, ksum, nb, norm_delta, box3, kf, mass,
                                                                stats, subtract_shot, pk_out, kmean_out);
+  GBP_LAUNCH_CHECK();
+  return GBP_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free binning.  Some callers cannot allocate device memory when
+// they call in: a JAX/XLA custom call (the way a JAX program would reach
+// this path) is handed only its operand and result buffers, and a host thread
+// that is recording the stream into a CUDA graph may not call cudaMalloc.
+// gbp_power_noalloc is gbp_power with its scratch (the per-group float-float
+// partial sums) in a fixed device array owned by the library, so the caller
+// passes only inputs and outputs.
+//
+// Limit: groups * moments * bins <= GBP_NOALLOC_PARTIALS float2 (16 MiB), e.g.
+// every 512^3 mesh with up to ~560 bins and l = 0,2,4.  Larger requests are
+// rejected with GBP_ERR_UNSUPPORTED before anything is launched.
+//
+// The array lives in every GPU that loads the library, until the process
+// exits.  Its device address is looked up once per device, with that device
+// current, the first time the entry point runs there; make that first call
+// before any stream capture.  All calls share the one array: calls whose
+// kernels overlap on the GPU (different streams, no ordering between them)
+// race on it.  Nothing needs clearing between calls: every partial the
+// reduce kernel reads is written earlier in the same call.
+namespace gbp {
+namespace {
+constexpr size_t GBP_NOALLOC_PARTIALS = (size_t)2 << 20;   // float2 entries (16 MiB)
+__device__ __align__(256) float2 g_noalloc_partials[GBP_NOALLOC_PARTIALS];
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_mutex;
+float2* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
+
+// Device address of the array on the current device (looked up once).
+int noalloc_partials(float2** out) {
+  int dev = 0;
+  GBP_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return GBP_ERR_UNSUPPORTED;
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partials);
+    if (e != cudaSuccess) {
+      set_last_cuda_error(e);
+      return GBP_ERR_CUDA;
+    }
+    g_noalloc_ptr[dev] = static_cast<float2*>(p);
+  }
+  *out = g_noalloc_ptr[dev];
+  return GBP_OK;
+}
+}  // namespace
+}  // namespace gbp
+
+extern "C" int gbp_power_noalloc(const void* spectrum, int G, int z_pitch, gbp_bins B, int mas_order, int ells,
+                                 const double* mass, double* sums_out, long long* nmodes_out, double* ksum_out,
+                                 gbp_stream_t stream_) {
+  cudaStream_t stream = reinterpret_cast<cudaStream_t>(stream_);
+  if (!spectrum || !B || !sums_out || !nmodes_out) return GBP_ERR_INVALID;
+  if (G != 1 && G != 2) return GBP_ERR_INVALID;
+  if (mas_order < 0 || mas_order > 8) return GBP_ERR_INVALID;
+  if ((ells & (GBP_ELL0 | GBP_ELL2 | GBP_ELL4)) == 0 || (ells & ~15)) return GBP_ERR_INVALID;
+  if ((ells & GBP_KSUM) && !ksum_out) return GBP_ERR_INVALID;
+  const int Lzs = z_pitch > 0 ? z_pitch : B->N / 2 + 1;
+  PowLayout L;
+  int st = power_layout(B, G, ells, Lzs, L);
+  if (st) return st;
+  if ((size_t)L.C * L.NV * B->nbe > GBP_NOALLOC_PARTIALS) return GBP_ERR_UNSUPPORTED;
+  float2* part_ff = nullptr;
+  st = noalloc_partials(&part_ff);
+  if (st) return st;
+
+  PowGeom g;
+  g.s0 = static_cast<const float2*>(spectrum);
+  g.s1 = G == 2 ? g.s0 + L.total : nullptr;
+  g.N = B->N;
+  g.Lz = B->N / 2 + 1;
+  g.Lzs = Lzs;
+  g.total = L.total;
+  g.chunk = L.chunk;
+  g.nb = B->nb;
+  g.nbe = B->nbe;
+  g.tu = B->last_closed;
+  g.lut_shift = B->lut_shift;
+  g.lut_n = B->lut_n;
+  g.mas_order = mas_order;
+  g.thr = B->d_thr;
+  g.lut = B->d_lut;
+  g.inv_sinc2 = B->d_inv_sinc2;
+  g.eph = B->d_eph;
+  g.zero_dc = mass != nullptr;
+  g.part_ff = part_ff;
+  g.warps = L.warps;
+  const bool aligned = ((reinterpret_cast<uintptr_t>(g.s0) | reinterpret_cast<uintptr_t>(g.s1)) & 15u) == 0;
+  const bool wide = L.wide && aligned;
+  void (*kern)(PowGeom) = nullptr;
+  const bool inter = G == 2;
+  if (L.NV == 1)
+    kern = wide ? (inter ? power_kernel<1, true, true> : power_kernel<1, false, true>)
+                : (inter ? power_kernel<1, true, false> : power_kernel<1, false, false>);
+  else if (L.NV == 2)
+    kern = wide ? (inter ? power_kernel<2, true, true> : power_kernel<2, false, true>)
+                : (inter ? power_kernel<2, true, false> : power_kernel<2, false, false>);
+  else
+    kern = wide ? (inter ? power_kernel<3, true, true> : power_kernel<3, false, true>)
+                : (inter ? power_kernel<3, true, false> : power_kernel<3, false, false>);
+  GBP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem));
+  int dev = 0, sms = 0, per_sm = 0;
+  GBP_CUDA_TRY(cudaGetDevice(&dev));
+  GBP_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  GBP_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, L.warps * 32, L.smem));
+  g.groups = L.C;
+  const int grid = std::max(1, std::min(L.C, sms * std::max(per_sm, 1)));
+  kern<<<grid, L.warps * 32, L.smem, stream>>>(g);
+  GBP_LAUNCH_CHECK();
+  const int wpb = 8;
+  power_reduce_kernel<<<(B->nb + wpb - 1) / wpb, wpb * 32, 0, stream>>>(
+      part_ff, L.C, L.NV, B->nb, B->nbe, B->d_nmodes, B->d_ksum, sums_out, nmodes_out,
+      (ells & GBP_KSUM) ? ksum_out : nullptr);
   GBP_LAUNCH_CHECK();
   return GBP_OK;
 }

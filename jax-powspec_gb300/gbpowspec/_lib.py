@@ -67,6 +67,7 @@ SIGNATURES = [
     ("gbp_power_workspace_size", _i, [_vp, _i, _i, _i, C.POINTER(_sz)]),
     ("gbp_power", _i, [_vp, _i, _i, _vp, _i, _i, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     ("gbp_power_normalize", _i, [_vp, _vp, _vp, _i, _i, _d, _vp, _vp, _i, _vp, _vp, _vp]),
+    ("gbp_power_noalloc", _i, [_vp, _i, _i, _vp, _i, _i, _vp, _vp, _vp, _vp, _vp]),
 ]
 
 _lock = threading.Lock()

@@ -1,0 +1,69 @@
+"""gbp_power_noalloc: binning without a caller-provided workspace.
+
+Some callers cannot allocate device memory when they call in -- a JAX/XLA
+custom call is handed only its operand and result buffers, and a thread that
+is recording its stream into a CUDA graph may not call cudaMalloc.  For them
+the library keeps the binning scratch in a fixed device array of its own.
+This test calls that entry point through the C ABI twice in a row and checks
+both results against gbp_power, which takes its scratch from the caller.
+It is collected last and passes alone in a fresh process as well.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def _spectrum():
+    """A real interlaced TSC spectrum (128^3 mesh, lognormal catalogue)."""
+    from gbpowspec import PkConfig, PowerSpectrum
+    from gbpowspec.synth import lognormal_catalogue
+    x, y, z = lognormal_catalogue(300_000, 1000.0, grid=64, seed=21)
+    ps = PowerSpectrum(PkConfig(n_mesh=128, box_size=1000.0, mas="tsc", interlace=True))
+    ps.run(*(torch.from_numpy(a).cuda() for a in (x, y, z)))
+    torch.cuda.synchronize()
+    return ps
+
+
+def test_noalloc_matches_workspace_entry_point_twice():
+    from gbpowspec import _lib, _native
+    lib = _lib.load()
+    ps = _spectrum()
+    dev = ps.spec.device
+    nb = ps.bins.n_bins
+    ells = _lib.ELL0 | _lib.ELL2 | _lib.ELL4 | _lib.KSUM
+    stream = C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+
+    want = _native.power(ps.spec, 2, ps.bins, mas_order=3, ells=ells, z_pitch=ps.plan.pitch, mass=ps.stats)
+    torch.cuda.synchronize()
+    for _ in range(2):
+        sums = torch.full((nb, 3), float("nan"), dtype=torch.float64, device=dev)
+        nmodes = torch.full((nb,), -1, dtype=torch.int64, device=dev)
+        ksum = torch.full((nb,), float("nan"), dtype=torch.float64, device=dev)
+        st = lib.gbp_power_noalloc(C.c_void_p(ps.spec.data_ptr()), 2, ps.plan.pitch, ps.bins.handle, 3, ells,
+                                   C.c_void_p(ps.stats.data_ptr()), C.c_void_p(sums.data_ptr()),
+                                   C.c_void_p(nmodes.data_ptr()), C.c_void_p(ksum.data_ptr()), stream)
+        assert st == 0, _lib.strerror(st)
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(nmodes.cpu().numpy(), want.nmodes.cpu().numpy())
+        np.testing.assert_allclose(sums.cpu().numpy(), want.sums.cpu().numpy(), rtol=1e-12, atol=0)
+        np.testing.assert_allclose(ksum.cpu().numpy(), want.ksum.cpu().numpy(), rtol=1e-12, atol=0)
+
+
+def test_noalloc_rejects_requests_beyond_its_array():
+    """A 1024^3 mesh with fine bins needs more than the fixed 16 MiB: refused before any launch."""
+    from gbpowspec import _lib, _native
+    lib = _lib.load()
+    dev = torch.device("cuda", 0)
+    edges = np.arange(0.5, 800.0, 0.5, dtype=np.float32)           # ~1600 bins in kF units
+    bins = _native.Bins(edges, 1024, dev)
+    dummy = torch.zeros(16, dtype=torch.float64, device=dev)
+    st = lib.gbp_power_noalloc(C.c_void_p(dummy.data_ptr()), 2, 1024 // 2 + 8, bins.handle, 3,
+                               _lib.ELL0 | _lib.ELL2 | _lib.ELL4, None, C.c_void_p(dummy.data_ptr()),
+                               C.c_void_p(dummy.data_ptr()), None,
+                               C.c_void_p(torch.cuda.current_stream(dev).cuda_stream))
+    assert st == _lib.GBP_ERR_UNSUPPORTED
+    bins.close()
