@@ -1,4 +1,4 @@
-"""Throughput benchmark: P_0,2,4(k) mocks/s on 512^3 TSC+interlaced lognormal mocks.
+"""Throughput benchmark: P_0,2,4(k) mocks/s on 512^3 TSC+interlaced lognormal mocks, batched vs plain.
 
 Workload (the configuration the headline metric is quoted on): 4,194,304
 float32 particles Poisson-like-sampled from a lognormal field on 256^3
@@ -9,11 +9,16 @@ Synthetic, seeded data (no survey catalogue is needed or used).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-One step = one mock through deposit -> FFT -> fused binning, particles
-already resident in HBM.  Every step streams ~4.4 GB of meshes and spectra,
-far more than the 129 MB L2, so no cache flush is needed between steps.
-Under torchrun each rank processes its own mocks (replicas, no collective
-on the data path); value = all ranks' mocks / max over ranks of the time.
+One step = one batch of `--batch` mocks through the batched path (lanes of
+resident buffers replaying one CUDA graph per mock, several lanes on their
+own streams), particles already resident in HBM; `value` is mocks/s of that
+path.  The plain path (one mock at a time through PowerSpectrum.run, no
+graph) is timed beside it.  Every mock streams ~4.4 GB of meshes and
+spectra, far more than the 129 MB L2, so no cache flush is needed between
+steps.  Per-kernel durations come from the library's CUDA-event trace of a
+few plain mocks.  Under torchrun each rank processes its own mocks
+(replicas, no collective on the data path); value = all ranks' mocks / max
+over ranks of the time.
 """
 from __future__ import annotations
 
@@ -147,11 +152,57 @@ def _cfg_json():
             "parallelism": "replicas"}
 
 
+def kernel_bytes(n: int, N: int, G: int) -> dict:
+    """Algorithmic bytes per launch of each traced kernel (what the algorithm must move)."""
+    M = N ** 3
+    Mh = N * N * (N // 2 + 1)
+    return {
+        "deposit_count": 12 * n,                  # read x, y, z
+        "deposit_scatter": 12 * n,                # read x, y, z (bucket writes are implementation traffic)
+        "deposit_tiles": 4 * G * M,               # write every cell of the G meshes once
+        "fft_z": G * (4 * M + 8 * Mh),            # read the meshes, write half-spectra
+        "fft_y": G * 16 * Mh,                     # read + write all grids' spectra
+        "fft_x": 16 * Mh,                         # read + write one grid's spectrum
+        "cufft_r2c": G * (4 * M + 8 * Mh),
+        "power_bins": G * 8 * Mh,                 # read the spectra once
+    }
+
+
+def trace_breakdown(ps, xd, yd, zd, reps: int, n: int) -> dict:
+    """Per-kernel mean durations (CUDA events on the launching stream) over `reps` plain mocks."""
+    import torch
+    from gbpowspec import _native
+    torch.cuda.synchronize()
+    _native.trace_enable(4096)
+    for _ in range(reps):
+        ps.run(xd, yd, zd)
+    recs = _native.trace_collect()
+    per = {}
+    for name, ms in recs:
+        d = per.setdefault(name, [0, 0.0])
+        d[0] += 1
+        d[1] += ms
+    N, G = ps.cfg.n_mesh, ps.cfg.grids
+    alg = kernel_bytes(n, N, G)
+    out = {}
+    for name, (cnt, tot) in per.items():
+        mean = tot / cnt
+        row = {"launches_per_mock": cnt / reps, "mean_ms": round(mean, 5), "ms_per_mock": round(tot / reps, 5)}
+        if name in alg:
+            row["algorithmic_bytes"] = alg[name]
+            row["achieved_gbs"] = round(alg[name] / (mean * 1e-3) / 1e9, 1)
+        out[name] = row
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=10, help="timed batches")
     ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--batch", type=int, default=16, help="mocks per batch (step)")
+    ap.add_argument("--lanes", type=int, default=0, help="lanes for the batched path (0 = tune among 1..3)")
+    ap.add_argument("--plain-steps", type=int, default=60)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--steps-ref", type=int, default=2)
     ap.add_argument("--warmup-ref", type=int, default=0)
@@ -159,7 +210,7 @@ def main():
     ap.add_argument("--n-mesh", type=int, default=None, help="override the mesh side (profiling cases)")
     ap.add_argument("--n-particles", type=int, default=None, help="override the particle count")
     ap.add_argument("--profile-only", action="store_true",
-                    help="warm-up + timed steps only (no stage/e2e/CPU legs): a short command for ncu")
+                    help="plain path only, warm-up + timed steps (no other legs): a short command for ncu")
     args = ap.parse_args()
     if args.n_mesh:
         CONFIG["n_mesh"] = args.n_mesh
@@ -179,7 +230,7 @@ def main():
     import torch.distributed as dist
 
     from gbpowspec import PkConfig, PowerSpectrum, algorithmic_bytes
-    from gbpowspec import _native
+    from gbpowspec.batch import BatchRunner, ParticleArena, tune_lanes
 
     ws, rank, local = _dist()
     torch.cuda.set_device(local)
@@ -187,113 +238,88 @@ def main():
     if ws > 1:
         dist.init_process_group("nccl", device_id=dev)
 
+    def barrier():
+        if ws > 1:
+            dist.barrier()
+
     x, y, z = make_catalogue(seed=1000 + rank)
     n = x.size
     host = [torch.from_numpy(a).pin_memory() for a in (x, y, z)]
     xd, yd, zd = (h.to(dev) for h in host)
     cfg = PkConfig(n_mesh=CONFIG["n_mesh"], box_size=CONFIG["box"], mas=CONFIG["mas"],
                    interlace=CONFIG["interlace"], ells=CONFIG["ells"])
+    N, G = cfg.n_mesh, cfg.grids
     ps = PowerSpectrum(cfg, dev)
     ps.reserve(n)
     stream = torch.cuda.current_stream(dev)
 
-    def barrier():
-        if ws > 1:
-            dist.barrier()
+    def timed(fn, steps):
+        barrier()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        barrier()
+        return e0.elapsed_time(e1) / 1e3
 
+    # ---- plain path: one mock at a time, resident buffers, no graph
     for _ in range(args.warmup):
         ps.run(xd, yd, zd)
-    torch.cuda.synchronize(dev)
-
-    # ---- headline: device-resident inputs
-    clocks = ClockSampler(local)
-    clocks.start()
-    barrier()
-    torch.cuda.synchronize(dev)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        ps.run(xd, yd, zd)
-    e1.record(stream)
-    torch.cuda.synchronize(dev)
-    barrier()
-    t_dev = e0.elapsed_time(e1) / 1e3
-    clk = clocks.stop()
     if args.profile_only:
+        t = timed(lambda: ps.run(xd, yd, zd), args.steps)
         if rank == 0:
-            print(json.dumps({"profile_only": True, "ms_per_step": t_dev / args.steps * 1e3,
-                              "config": _cfg_json()}), flush=True)
+            print(json.dumps({"profile_only": True, "ms_per_step": t / args.steps * 1e3, "config": _cfg_json()}),
+                  flush=True)
         if ws > 1:
             dist.destroy_process_group()
         return
+    t_plain = timed(lambda: ps.run(xd, yd, zd), args.plain_steps)
 
-    # ---- stage breakdown (instrumented loop, events between the stages)
-    N, G = cfg.n_mesh, cfg.grids
-    stage_names = ["deposit", "fft", "power", "normalize"]
-    acc = {s: 0.0 for s in stage_names}
-    reps = max(3, min(args.steps, 10))
-    import ctypes as C
-    from gbpowspec import _lib
-    inv = np.float32(N / cfg.box_size)
-    for _ in range(reps):
-        ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
-        ev[0].record(stream)
-        _native.deposit(xd, yd, zd, None, n_mesh=N, inv_cell=inv, origin=cfg.origin, mas=cfg.mas_order,
-                        interlace=cfg.interlace, compat=0, wrap=True, out=ps.mesh, stats=ps.stats,
-                        ws=ps._dep_ws(n))
-        ev[1].record(stream)
-        ps.plan.execute(ps.mesh, ps.spec, ps.fft_ws)
-        ev[2].record(stream)
-        _native.power(ps.spec, G, ps.bins, mas_order=cfg.mas_order, ells=ps.ells, z_pitch=ps.plan.pitch,
-                      mass=ps.stats, ws=ps.pow_ws,
-                      out=ps.sums)
-        ev[3].record(stream)
-        _native.normalize(ps.sums, n_mesh=N, box_size=cfg.box_size, mass=ps.stats, stats=ps.stats,
-                          subtract_shot=cfg.shot_noise, pk_out=ps.pk, kmean_out=ps.kmean)
-        ev[4].record(stream)
-        torch.cuda.synchronize(dev)
-        for i, s in enumerate(stage_names):
-            acc[s] += ev[i].elapsed_time(ev[i + 1]) / 1e3
-    stage = {s: acc[s] / reps for s in stage_names}
-    Mh = N * N * (N // 2 + 1)
-    alg = {"deposit": n * 12 + G * 4 * N ** 3, "fft": G * (4 * N ** 3 + 8 * Mh), "power": G * 8 * Mh}
-    dom = max(alg, key=lambda s: stage[s])
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except OSError:
-        pass
-    peak = float(peaks.get("hbm_gbs", 6800.0))
-    achieved = alg[dom] / stage[dom] / 1e9
+    # ---- per-kernel trace of a few plain mocks (CUDA events around every launch)
+    kernels = trace_breakdown(ps, xd, yd, zd, reps=5, n=n)
 
-    # ---- end to end: pinned host particles -> device, pipeline, P_l back to host
-    pk_host = torch.empty(ps.pk.shape, dtype=ps.pk.dtype, pin_memory=True)
-    nm_host = torch.empty(ps.sums.nmodes.shape, dtype=torch.int64, pin_memory=True)
+    # ---- batched path: B mocks per step (two distinct catalogues, each mock its own slice of the arena)
+    B = args.batch
+    x2, y2, z2 = make_catalogue(seed=2000 + rank)
+    cats = [(x, y, z) if i % 2 == 0 else (x2, y2, z2) for i in range(B)]
+    arena = ParticleArena(cats, device=dev)
+    arena.upload()
+    jobs = arena.job_table(cfg.box_size, N)
+    kw = dict(capacity=n, mas=cfg.mas, interlace=cfg.interlace, ells=cfg.ells, kedges_grid=cfg.kedges_grid())
+    lane_rates = None
+    if args.lanes > 0:
+        lanes = args.lanes
+    else:
+        lanes, lane_rates = tune_lanes(N, jobs, candidates=(1, 2, 3), repeats=1, **kw)
+    runner = BatchRunner(N, n_lanes=lanes, device=dev, **kw)
+    res = runner.alloc_result(B)
+    for _ in range(args.warmup):
+        runner.run(jobs, res)
+    clocks = ClockSampler(local)
+    clocks.start()
+    t_batch = timed(lambda: runner.run(jobs, res), args.steps)
+    clk = clocks.stop()
+
+    # ---- end to end through the batched API: pinned host particles -> device, P_l back to host
+    pk_host = torch.empty(res.pk.shape, dtype=res.pk.dtype, pin_memory=True)
+
+    def e2e_step():
+        arena.upload()
+        runner.run(jobs, res)
+        pk_host.copy_(res.pk, non_blocking=True)
+
     for _ in range(2):
-        for h, d in zip(host, (xd, yd, zd)):
-            d.copy_(h, non_blocking=True)
-        ps.run(xd, yd, zd)
-        pk_host.copy_(ps.pk, non_blocking=True)
-    torch.cuda.synchronize(dev)
-    barrier()
-    e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e2.record(stream)
-    for _ in range(args.steps):
-        for h, d in zip(host, (xd, yd, zd)):
-            d.copy_(h, non_blocking=True)
-        r = ps.run(xd, yd, zd)
-        pk_host.copy_(r.pk, non_blocking=True)
-        nm_host.copy_(r.nmodes, non_blocking=True)
-    e3.record(stream)
-    torch.cuda.synchronize(dev)
-    barrier()
-    t_e2e = e2.elapsed_time(e3) / 1e3
+        e2e_step()
+    t_e2e = timed(e2e_step, args.steps)
 
     # max over ranks
-    times = torch.tensor([t_dev, t_e2e], dtype=torch.float64, device=dev)
+    times = torch.tensor([t_batch, t_e2e, t_plain], dtype=torch.float64, device=dev)
     if ws > 1:
         dist.all_reduce(times, op=dist.ReduceOp.MAX)
-    t_dev, t_e2e = float(times[0]), float(times[1])
+    t_batch, t_e2e, t_plain = (float(v) for v in times)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -302,31 +328,56 @@ def main():
                "sample": "one full 512^3 / 4,194,304-particle mock of the reference path (CIC, no interlacing) "
                          "through the numpy port of src/mas.py + src/correlations.py"}
 
-    mocks = ws * args.steps
-    kernels_per_mock = 7   # count, scatter, tile deposit, stats, power, fold, normalize (cub scan/cuFFT excluded)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    timed_k = {k: v for k, v in kernels.items() if "algorithmic_bytes" in v}
+    dom = max(timed_k, key=lambda k: timed_k[k]["ms_per_mock"])
+    ach = timed_k[dom]["achieved_gbs"]
+    traffic = PROFILED_TRAFFIC.get((dom, N, n))
+
+    mocks = ws * args.steps * B
+    per_mock_launches = sum(v["launches_per_mock"] for v in kernels.values())
     line = {
-        "metric": METRIC, "value": mocks / t_dev, "unit": "mocks/s", "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": t_dev / args.steps * 1e3, "higher_is_better": True,
+        "metric": METRIC, "value": mocks / t_batch, "unit": "mocks/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_batch / args.steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded lognormal+RSD mocks)",
-        "config": {**_cfg_json(), "path": "plain (one mock per step, resident PowerSpectrum)"},
-        "particles_per_s": mocks * n / t_dev,
-        "stages_ms": {s: round(v * 1e3, 4) for s, v in stage.items()},
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None,
-                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800 GB/s",
-                     "algorithmic_bytes": alg[dom]},
+        "config": {**_cfg_json(), "path": f"batched: {B} mocks per step over {lanes} lanes (one CUDA graph "
+                                          "replay per mock, lanes on their own streams)",
+                   "batch": B, "lanes": lanes, "lane_tuning_mocks_per_s": lane_rates},
+        "particles_per_s": mocks * n / t_batch,
+        "plain": {"value": ws * args.plain_steps / t_plain, "unit": "mocks/s", "steps": args.plain_steps,
+                  "ms_per_mock": t_plain / args.plain_steps * 1e3,
+                  "path": "PowerSpectrum.run, one mock at a time, no graph"},
+        "batched_over_plain": (mocks / t_batch) / (ws * args.plain_steps / t_plain),
+        "kernels": kernels,
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s",
+                     "frac": ach / peak, "traffic": traffic,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6800 GB/s",
+                     "algorithmic_bytes": timed_k[dom]["algorithmic_bytes"]},
         "pipeline_roofline": {"algorithmic_bytes_per_mock": algorithmic_bytes(n, N, G),
-                              "frac": algorithmic_bytes(n, N, G) * mocks / ws / t_dev / 1e9 / peak},
+                              "frac": algorithmic_bytes(n, N, G) * mocks / ws / t_batch / 1e9 / peak},
         "cpu_baseline": cpu,
-        "e2e": {"value": mocks / t_e2e, "unit": "mocks/s", "h2d_bytes_per_step": 3 * 4 * n,
-                "d2h_bytes_per_step": int(pk_host.numel() * 8 + nm_host.numel() * 8)},
-        "gpu_launches": kernels_per_mock * args.steps,
+        "e2e": {"value": mocks / t_e2e, "unit": "mocks/s", "h2d_bytes_per_step": arena.nbytes,
+                "d2h_bytes_per_step": int(pk_host.numel() * 8),
+                "path": "ParticleArena.upload (pinned H2D of every mock) + BatchRunner.run + P_l D2H"},
+        "gpu_launches": int(round(per_mock_launches)) * args.steps * B + lanes * args.steps,
         "clocks": clk,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:
         dist.destroy_process_group()
+
+
+# DRAM bytes (read + write) per launch from ncu captures of the same kernels
+# (--set full, --clock-control none), keyed by (kernel, mesh, particles).
+PROFILED_TRAFFIC = {
+    ("deposit_tiles", 512, 4_194_304): 1_123_164_000,
+}
 
 
 if __name__ == "__main__":

@@ -95,6 +95,31 @@ typedef struct gbp_deposit_stats {
 int gbp_deposit_workspace_size(int64_t n_particles, int n_mesh, int mas,
                                int interlace, int compat, size_t* bytes);
 
+/* A mock described in DEVICE memory, so that a captured CUDA graph can be
+ * replayed for a different mock by rewriting these bytes (no new graph):
+ * particles, their count, and the box geometry.  inv_cell, xmin.. as for
+ * gbp_deposit; box_size feeds gbp_power_normalize_job.  No reference
+ * counterpart (the reference has no batching). */
+typedef struct gbp_job {
+  const float* x;
+  const float* y;
+  const float* z;
+  const float* w;       /* NULL = unit weights */
+  long long n;          /* <= the capacity the kernels were sized for */
+  float inv_cell, xmin, ymin, zmin;
+  double box_size;
+} gbp_job;
+
+/* gbp_deposit for a mock held in a device gbp_job (B-spline schemes only,
+ * compat = GBP_COMPAT_NONE).  Launch sizes and the workspace
+ * (gbp_deposit_workspace_size(capacity, ...)) depend only on `capacity`,
+ * never on job->n; particles past `capacity` are not deposited (n_kept in
+ * the statistics says how many were). */
+int gbp_deposit_job(const gbp_job* job, int64_t capacity, int n_mesh, int mas,
+                    int interlace, float* mesh_out,
+                    gbp_deposit_stats* stats_out, void* workspace,
+                    size_t workspace_bytes, gbp_stream_t stream);
+
 int gbp_deposit(const float* x, const float* y, const float* z, const float* w,
                 int64_t n_particles, float xmin, float ymin, float zmin,
                 float inv_cell, int n_mesh, int mas, int interlace, int compat,
@@ -218,6 +243,67 @@ int gbp_power_normalize(const double* sums, const long long* nmodes,
                         const gbp_deposit_stats* stats, int subtract_shot,
                         double* pk_out, double* kmean_out,
                         gbp_stream_t stream);
+
+/* gbp_power_normalize with the box size read from a device gbp_job. */
+int gbp_power_normalize_job(const double* sums, const long long* nmodes,
+                            const double* ksum, int n_bins, int n_mesh,
+                            const gbp_job* job, const double* mass,
+                            const gbp_deposit_stats* stats, int subtract_shot,
+                            double* pk_out, double* kmean_out,
+                            gbp_stream_t stream);
+
+/* ---- Lanes: resident per-mock pipelines for batching and serving --------
+ * No reference counterpart (the reference computes one mock per call).
+ * A lane owns every buffer one mock needs and, with GBP_LANE_GRAPH, a CUDA
+ * graph of the whole sequence (job slot <- table[cursor]; deposit; FFT;
+ * binning; normalisation; outputs -> caller arrays at cursor; cursor +=
+ * stride).  Jobs and outputs are addressed through device memory, so the
+ * same graph is replayed for every mock.  A lane serves one job at a time:
+ * calls on one lane must be ordered (same stream, or joined streams). */
+typedef struct gbp_lane_s* gbp_lane;
+
+#define GBP_LANE_GRAPH 1   /* capture the launch sequence into a CUDA graph */
+
+/* Per-job outputs (device pointers, any may be NULL), indexed by job j:
+ * pk[(j*nb + b)*3 + l] (l = 0,2,4 -> 0,1,2), kmean[j*nb + b],
+ * nmodes[j*nb + b], stats[j]. */
+typedef struct gbp_lane_out {
+  double* pk;
+  double* kmean;
+  long long* nmodes;
+  gbp_deposit_stats* stats;
+} gbp_lane_out;
+
+/* Device bytes a lane of this shape holds (for admission against a budget). */
+int gbp_lane_bytes(int n_mesh, int mas, int interlace, int ells, gbp_bins bins,
+                   int64_t capacity, size_t* bytes);
+/* bins: borrowed, must outlive the lane; capacity: most particles per job. */
+int gbp_lane_create(int n_mesh, int mas, int interlace, int ells,
+                    int shot_noise, gbp_bins bins, int64_t capacity, int flags,
+                    gbp_lane* lane);
+int gbp_lane_info(gbp_lane lane, size_t* bytes, int* n_bins, int* graph);
+int gbp_lane_destroy(gbp_lane lane);
+/* Runs jobs first, first+stride, ... < n_jobs of the device table `jobs` on
+ * `stream`, in order. */
+int gbp_lane_run(gbp_lane lane, const gbp_job* jobs, int n_jobs, int first,
+                 int stride, const gbp_lane_out* out, gbp_stream_t stream);
+/* Splits n_jobs round-robin over n_lanes distinct lanes of one shape, each on
+ * its own stream forked from and joined back into `stream`. */
+int gbp_batch_run(gbp_lane* lanes, int n_lanes, const gbp_job* jobs,
+                  int n_jobs, const gbp_lane_out* out, gbp_stream_t stream);
+
+/* ---- Kernel tracing (no reference counterpart) ---------------------------
+ * While enabled, every kernel the library launches outside stream capture is
+ * bracketed by CUDA events on its stream.  gbp_trace_collect stops tracing,
+ * waits for the recorded launches and returns their names (static strings)
+ * and durations in ms, in launch order. */
+typedef struct gbp_trace_record {
+  const char* kernel;
+  float ms;
+} gbp_trace_record;
+
+int gbp_trace_enable(int capacity);
+int gbp_trace_collect(gbp_trace_record* out, int max_records, int* n_records);
 
 #ifdef __cplusplus
 }

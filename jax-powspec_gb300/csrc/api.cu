@@ -292,6 +292,7 @@ extern "C" int gbp_fft_r2c(gbp_fft_plan p, const float* mesh, void* spec, void* 
   if (cufftSetStream(p->h, reinterpret_cast<cudaStream_t>(stream)) != CUFFT_SUCCESS) return GBP_ERR_CUFFT;
   if (p->ws > 0 && cufftSetWorkArea(p->h, ws) != CUFFT_SUCCESS) return GBP_ERR_CUFFT;
   // Out-of-place R2C leaves its input untouched; cuFFT's prototype is non-const.
+  GBP_TRACE("cufft_r2c", reinterpret_cast<cudaStream_t>(stream));
   if (cufftExecR2C(p->h, const_cast<cufftReal*>(mesh), static_cast<cufftComplex*>(spec)) != CUFFT_SUCCESS)
     return GBP_ERR_CUFFT;
   return GBP_OK;

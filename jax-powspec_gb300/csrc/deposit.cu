@@ -49,7 +49,20 @@ struct DepGeom {
   int tshift;       // log2(tdim) when tdim is a power of two, else -1
   int nt;           // tiles per axis
   int vec_ok;       // mesh pointers are 16-byte aligned (float4 tile stores allowed)
+  const gbp_job* job;  // non-null: particles, n and box geometry are read from here
+  long long cap;       // job mode: the capacity the launches were sized for
 };
+
+// Job mode: the particle pointers, count and box geometry come from a
+// gbp_job in device memory (one broadcast load per thread), so the launch
+// parameters do not depend on the mock.
+__device__ __forceinline__ void resolve_job(DepGeom& g) {
+  if (!g.job) return;
+  const gbp_job j = *g.job;
+  g.x = j.x; g.y = j.y; g.z = j.z; g.w = j.w;
+  g.n = j.n < 0 ? 0 : (j.n > g.cap ? g.cap : j.n);   // the buckets hold `cap` particles at most
+  g.ox = j.xmin; g.oy = j.ymin; g.oz = j.zmin; g.inv_cell = j.inv_cell;
+}
 
 // Node index reduced into [0, N).  Stencil nodes lie within a few cells of
 // [0, N); tiny meshes fall back to the general modulo.
@@ -235,17 +248,17 @@ __device__ __forceinline__ ff warp_ff_sum(ff v) {
 }
 
 struct DepCounters {           // zeroed by one memset per call
-  unsigned long long mass_fixed[2];
-  unsigned long long n_kept;
-  unsigned long long n_nonfinite;
   unsigned int maxw_bits;
-  unsigned int pad_;
+  unsigned int pad_[3];
 };
 
 // Pass 1: tile occupancy counts + weight statistics.
 template <int MAS, int G, int CM>
 __global__ void __launch_bounds__(CNT_THREADS)
-count_kernel(DepGeom g, unsigned* __restrict__ counts, DepCounters* ctr, float4* block_stats) {
+count_kernel(DepGeom gp, unsigned* __restrict__ counts, DepCounters* ctr, float4* block_stats,
+             uint2* block_counts) {
+  DepGeom g = gp;
+  resolve_job(g);
   float maxw = 0.0f;
   ff sw{0.f, 0.f}, sw2{0.f, 0.f};
   unsigned kept = 0, bad = 0;
@@ -294,16 +307,17 @@ count_kernel(DepGeom g, unsigned* __restrict__ counts, DepCounters* ctr, float4*
       b = ff_add(b, s_sw2[k]);
     }
     block_stats[blockIdx.x] = make_float4(a.hi, a.lo, b.hi, b.lo);
+    block_counts[blockIdx.x] = make_uint2(s_kept, s_bad);
     if (m > 0.f) atomicMax(&ctr->maxw_bits, __float_as_uint(m));
-    if (s_kept) atomicAdd(&ctr->n_kept, (unsigned long long)s_kept);
-    if (s_bad) atomicAdd(&ctr->n_nonfinite, (unsigned long long)s_bad);
   }
 }
 
 // Pass 3: append (u_x, u_y, u_z, w) to every touched tile's bucket.
 template <int MAS, int G, int CM>
 __global__ void __launch_bounds__(CNT_THREADS)
-scatter_kernel(DepGeom g, unsigned* __restrict__ cursors, float4* __restrict__ entries) {
+scatter_kernel(DepGeom gp, unsigned* __restrict__ cursors, float4* __restrict__ entries) {
+  DepGeom g = gp;
+  resolve_job(g);
   Batch bt;
   load_batch(g, bt);
 #pragma unroll
@@ -370,10 +384,11 @@ __device__ __forceinline__ void local_nodes(const Axis<R>& a, int N, int t0, int
 template <int MAS, int G, int CM>
 __global__ void __launch_bounds__(DEP_THREADS)
 deposit_kernel(DepGeom g, const float4* __restrict__ entries, const unsigned* __restrict__ counts,
-               const unsigned* __restrict__ cursors, DepCounters* ctr, const float* __restrict__ mesh_in,
-               float* __restrict__ mesh_out) {
+               const unsigned* __restrict__ cursors, const DepCounters* ctr, const float* __restrict__ mesh_in,
+               float* __restrict__ mesh_out, long long* __restrict__ tile_mass) {
   constexpr int R = Scheme<MAS, CM>::R;
   extern __shared__ __align__(16) unsigned acc32[];
+  __shared__ long long s_part[DEP_THREADS / 32];
   unsigned* lo = acc32;
   unsigned* hi = acc32 + TILE3;
   const int t = blockIdx.x;
@@ -476,37 +491,70 @@ deposit_kernel(DepGeom g, const float4* __restrict__ entries, const unsigned* __
       }
     }
     for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-    if ((threadIdx.x & 31) == 0 && part != 0)
-      atomicAdd(&ctr->mass_fixed[grid], static_cast<unsigned long long>(part));
+    if ((threadIdx.x & 31) == 0) s_part[threadIdx.x >> 5] = part;
     __syncthreads();                            // the next grid reuses the accumulators
+    if (threadIdx.x == 0) {                     // this tile's exact total (read by stats_kernel)
+      long long tm = 0;
+      for (int k = 0; k < DEP_THREADS / 32; ++k) tm += s_part[k];
+      tile_mass[(long long)grid * gridDim.x + t] = tm;
+    }
   }
 }
 
-// Pass 5: fold the per-block statistics (fixed order) into gbp_deposit_stats.
-__global__ void stats_kernel(const DepCounters* ctr, const float4* block_stats, int nblocks, long long n,
-                             int compat, int G, gbp_deposit_stats* out) {
+// Pass 5: fold the per-block statistics and the per-tile mass totals into
+// gbp_deposit_stats.  Float partials are folded in a fixed order; integer
+// totals are exact in any order.
+constexpr int STATS_THREADS = 1024;
+__global__ void __launch_bounds__(STATS_THREADS)
+stats_kernel(const DepCounters* ctr, const float4* block_stats, const uint2* block_counts, int nblocks,
+             const long long* tile_mass, int ntiles, int compat, int G, gbp_deposit_stats* out) {
   __shared__ ff s_a[32], s_b[32];
+  __shared__ long long s_m[2][32], s_c[2][32];
   ff a{0.f, 0.f}, b{0.f, 0.f};
+  long long kept = 0, bad = 0, m0 = 0, m1 = 0;
   for (int k = threadIdx.x; k < nblocks; k += blockDim.x) {
     const float4 v = block_stats[k];
     a = ff_add(a, ff{v.x, v.y});
     b = ff_add(b, ff{v.z, v.w});
+    const uint2 c = block_counts[k];
+    kept += c.x;
+    bad += c.y;
+  }
+  for (int k = threadIdx.x; k < ntiles; k += blockDim.x) {
+    m0 += tile_mass[k];
+    if (G == 2) m1 += tile_mass[ntiles + k];
   }
   a = warp_ff_sum(a);
   b = warp_ff_sum(b);
-  if ((threadIdx.x & 31) == 0) { s_a[threadIdx.x >> 5] = a; s_b[threadIdx.x >> 5] = b; }
+  for (int o = 16; o > 0; o >>= 1) {
+    kept += __shfl_xor_sync(0xffffffffu, kept, o);
+    bad += __shfl_xor_sync(0xffffffffu, bad, o);
+    m0 += __shfl_xor_sync(0xffffffffu, m0, o);
+    m1 += __shfl_xor_sync(0xffffffffu, m1, o);
+  }
+  const int wid = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    s_a[wid] = a; s_b[wid] = b;
+    s_c[0][wid] = kept; s_c[1][wid] = bad;
+    s_m[0][wid] = m0; s_m[1][wid] = m1;
+  }
   __syncthreads();
   if (threadIdx.x == 0) {
     ff ta{0.f, 0.f}, tb{0.f, 0.f};
-    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) { ta = ff_add(ta, s_a[k]); tb = ff_add(tb, s_b[k]); }
+    long long tk = 0, tbad = 0, tm[2] = {0, 0};
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+      ta = ff_add(ta, s_a[k]);
+      tb = ff_add(tb, s_b[k]);
+      tk += s_c[0][k]; tbad += s_c[1][k];
+      tm[0] += s_m[0][k]; tm[1] += s_m[1][k];
+    }
     const int s = fixed_scale_exp(ctr->maxw_bits, compat);
     const double inv = ldexp(1.0, -s);
-    for (int grid = 0; grid < 2; ++grid)
-      out->mass[grid] = grid < G ? (double)(long long)ctr->mass_fixed[grid] * inv : 0.0;
+    for (int grid = 0; grid < 2; ++grid) out->mass[grid] = grid < G ? (double)tm[grid] * inv : 0.0;
     out->sum_w = (double)ta.hi + (double)ta.lo;
     out->sum_w2 = (double)tb.hi + (double)tb.lo;
-    out->n_kept = (long long)ctr->n_kept;
-    out->n_nonfinite = (long long)ctr->n_nonfinite;
+    out->n_kept = tk;
+    out->n_nonfinite = tbad;
     out->scale_exp = s;
     out->pad_ = 0;
   }
@@ -554,8 +602,9 @@ int deposit_layout(int64_t n, int N, int mas, int interlace, int compat, DepLayo
   L.nblocks = (int)((n + (long long)CNT_THREADS * CNT_ITEMS - 1) / ((long long)CNT_THREADS * CNT_ITEMS));
   L.scan_bytes = 0;
   cub::DeviceScan::ExclusiveSum(nullptr, L.scan_bytes, (unsigned*)nullptr, (unsigned*)nullptr, L.ntiles);
-  L.total = align256(sizeof(DepCounters)) + align256((size_t)L.ntiles * 4) * 2 +
-            align256((size_t)(L.nblocks > 0 ? L.nblocks : 1) * sizeof(float4)) +
+  const size_t nbl = (size_t)(L.nblocks > 0 ? L.nblocks : 1);
+  L.total = align256(sizeof(DepCounters)) + align256((size_t)L.ntiles * 4) * 2 + align256(nbl * sizeof(float4)) +
+            align256(nbl * sizeof(uint2)) + align256((size_t)L.ntiles * 2 * sizeof(long long)) +
             align256((size_t)n * L.maxrep * sizeof(float4) + 16) + align256(L.scan_bytes);
   return GBP_OK;
 }
@@ -567,6 +616,8 @@ struct Launch {
   unsigned* cursors;
   DepCounters* ctr;
   float4* block_stats;
+  uint2* block_counts;
+  long long* tile_mass;
   float4* entries;
   void* scan_tmp;
   const float* mesh_in;
@@ -578,12 +629,18 @@ template <int MAS, int G, int CM>
 int run_scheme(const Launch& q) {
   const DepLayout& L = *q.L;
   if (L.nblocks > 0) {
-    count_kernel<MAS, G, CM><<<L.nblocks, CNT_THREADS, 0, q.stream>>>(q.g, q.counts, q.ctr, q.block_stats);
+    GBP_TRACE("deposit_count", q.stream);
+    count_kernel<MAS, G, CM><<<L.nblocks, CNT_THREADS, 0, q.stream>>>(q.g, q.counts, q.ctr, q.block_stats,
+                                                                     q.block_counts);
     GBP_LAUNCH_CHECK();
   }
-  size_t scan_bytes = L.scan_bytes;
-  GBP_CUDA_TRY(cub::DeviceScan::ExclusiveSum(q.scan_tmp, scan_bytes, q.counts, q.cursors, L.ntiles, q.stream));
+  {
+    GBP_TRACE("deposit_scan", q.stream);
+    size_t scan_bytes = L.scan_bytes;
+    GBP_CUDA_TRY(cub::DeviceScan::ExclusiveSum(q.scan_tmp, scan_bytes, q.counts, q.cursors, L.ntiles, q.stream));
+  }
   if (L.nblocks > 0) {
+    GBP_TRACE("deposit_scatter", q.stream);
     scatter_kernel<MAS, G, CM><<<L.nblocks, CNT_THREADS, 0, q.stream>>>(q.g, q.cursors, q.entries);
     GBP_LAUNCH_CHECK();
   }
@@ -591,9 +648,65 @@ int run_scheme(const Launch& q) {
   // more than 48 KB of dynamic shared memory needs the opt-in (cheap, per call)
   GBP_CUDA_TRY(cudaFuncSetAttribute(deposit_kernel<MAS, G, CM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)smem));
-  deposit_kernel<MAS, G, CM><<<L.ntiles, DEP_THREADS, smem, q.stream>>>(q.g, q.entries, q.counts, q.cursors,
-                                                                       q.ctr, q.mesh_in, q.mesh_out);
-  GBP_LAUNCH_CHECK();
+  {
+    GBP_TRACE("deposit_tiles", q.stream);
+    deposit_kernel<MAS, G, CM><<<L.ntiles, DEP_THREADS, smem, q.stream>>>(q.g, q.entries, q.counts, q.cursors,
+                                                                         q.ctr, q.mesh_in, q.mesh_out, q.tile_mass);
+    GBP_LAUNCH_CHECK();
+  }
+  return GBP_OK;
+}
+
+// Carve the workspace, launch the scheme's kernels, fold the statistics.
+// `n` sizes the launches (the particle count, or a job's capacity).
+int deposit_launch(DepGeom g, const DepLayout& L, int64_t n, int mas, int G, int compat, const float* mesh_in,
+                   float* mesh_out, gbp_deposit_stats* stats_out, void* workspace, cudaStream_t stream) {
+  Carver cv(workspace);
+  Launch q;
+  const int nbl = L.nblocks > 0 ? L.nblocks : 1;
+  q.ctr = cv.take<DepCounters>(1);
+  q.counts = cv.take<unsigned>(L.ntiles);
+  q.cursors = cv.take<unsigned>(L.ntiles);
+  q.block_stats = cv.take<float4>(nbl);
+  q.block_counts = cv.take<uint2>(nbl);
+  q.tile_mass = cv.take<long long>((size_t)L.ntiles * 2);
+  q.entries = cv.take<float4>((size_t)n * L.maxrep + 1);
+  q.scan_tmp = cv.take<char>(L.scan_bytes);
+  q.L = &L;
+  q.mesh_in = mesh_in;
+  q.mesh_out = mesh_out;
+  q.stream = stream;
+  g.tdim = L.tdim; g.tshift = L.tshift; g.nt = L.nt;
+  g.vec_ok = ((reinterpret_cast<uintptr_t>(mesh_out) | reinterpret_cast<uintptr_t>(mesh_in)) & 15u) == 0;
+  q.g = g;
+
+  // counters + tile counts are adjacent: one memset clears both.
+  GBP_CUDA_TRY(cudaMemsetAsync(q.ctr, 0, align256(sizeof(DepCounters)) + align256((size_t)L.ntiles * 4), stream));
+  int st;
+  if (compat == GBP_COMPAT_VEC) st = run_scheme<GBP_CIC, 1, GBP_COMPAT_VEC>(q);
+  else if (compat == GBP_COMPAT_SCAN) st = run_scheme<GBP_CIC, 1, GBP_COMPAT_SCAN>(q);
+  else if (G == 1) {
+    switch (mas) {
+      case GBP_NGP: st = run_scheme<GBP_NGP, 1, 0>(q); break;
+      case GBP_CIC: st = run_scheme<GBP_CIC, 1, 0>(q); break;
+      case GBP_TSC: st = run_scheme<GBP_TSC, 1, 0>(q); break;
+      default: st = run_scheme<GBP_PCS, 1, 0>(q); break;
+    }
+  } else {
+    switch (mas) {
+      case GBP_NGP: st = run_scheme<GBP_NGP, 2, 0>(q); break;
+      case GBP_CIC: st = run_scheme<GBP_CIC, 2, 0>(q); break;
+      case GBP_TSC: st = run_scheme<GBP_TSC, 2, 0>(q); break;
+      default: st = run_scheme<GBP_PCS, 2, 0>(q); break;
+    }
+  }
+  if (st) return st;
+  if (stats_out) {
+    GBP_TRACE("deposit_stats", stream);
+    stats_kernel<<<1, STATS_THREADS, 0, stream>>>(q.ctr, q.block_stats, q.block_counts, L.nblocks, q.tile_mass,
+                                                  L.ntiles, compat, G, stats_out);
+    GBP_LAUNCH_CHECK();
+  }
   return GBP_OK;
 }
 
@@ -617,57 +730,33 @@ extern "C" int gbp_deposit(const float* x, const float* y, const float* z, const
                            int interlace, int compat, int wrap, const float* mesh_in, float* mesh_out,
                            gbp_deposit_stats* stats_out, void* workspace, size_t ws_bytes,
                            gbp_stream_t stream_) {
-  cudaStream_t stream = reinterpret_cast<cudaStream_t>(stream_);
   DepLayout L;
-  int st = deposit_layout(n, N, mas, interlace, compat, L);
+  const int st = deposit_layout(n, N, mas, interlace, compat, L);
   if (st) return st;
   if (!mesh_out) return GBP_ERR_INVALID;
   if (n > 0 && (!x || !y || !z)) return GBP_ERR_INVALID;
   if (!workspace || ws_bytes < L.total) return GBP_ERR_WORKSPACE;
-
-  Carver cv(workspace);
-  Launch q;
-  q.ctr = cv.take<DepCounters>(1);
-  q.counts = cv.take<unsigned>(L.ntiles);
-  q.cursors = cv.take<unsigned>(L.ntiles);
-  q.block_stats = cv.take<float4>(L.nblocks > 0 ? L.nblocks : 1);
-  q.entries = cv.take<float4>((size_t)n * L.maxrep + 1);
-  q.scan_tmp = cv.take<char>(L.scan_bytes);
-  q.L = &L;
-  q.mesh_in = mesh_in;
-  q.mesh_out = mesh_out;
-  q.stream = stream;
-  const int G = interlace ? 2 : 1;
-  DepGeom& g = q.g;
+  DepGeom g{};
   g.x = x; g.y = y; g.z = z; g.w = w; g.n = n;
   g.ox = xmin; g.oy = ymin; g.oz = zmin; g.inv_cell = inv_cell;
   g.N = N; g.wrap = wrap ? 1 : 0;
-  g.tdim = L.tdim; g.tshift = L.tshift; g.nt = L.nt;
-  g.vec_ok = ((reinterpret_cast<uintptr_t>(mesh_out) | reinterpret_cast<uintptr_t>(mesh_in)) & 15u) == 0;
+  g.job = nullptr;
+  return deposit_launch(g, L, n, mas, interlace ? 2 : 1, compat, mesh_in, mesh_out, stats_out, workspace,
+                        reinterpret_cast<cudaStream_t>(stream_));
+}
 
-  // counters + tile counts are adjacent: one memset clears both.
-  GBP_CUDA_TRY(cudaMemsetAsync(q.ctr, 0, align256(sizeof(DepCounters)) + align256((size_t)L.ntiles * 4), stream));
-  if (compat == GBP_COMPAT_VEC) st = run_scheme<GBP_CIC, 1, GBP_COMPAT_VEC>(q);
-  else if (compat == GBP_COMPAT_SCAN) st = run_scheme<GBP_CIC, 1, GBP_COMPAT_SCAN>(q);
-  else if (G == 1) {
-    switch (mas) {
-      case GBP_NGP: st = run_scheme<GBP_NGP, 1, 0>(q); break;
-      case GBP_CIC: st = run_scheme<GBP_CIC, 1, 0>(q); break;
-      case GBP_TSC: st = run_scheme<GBP_TSC, 1, 0>(q); break;
-      default: st = run_scheme<GBP_PCS, 1, 0>(q); break;
-    }
-  } else {
-    switch (mas) {
-      case GBP_NGP: st = run_scheme<GBP_NGP, 2, 0>(q); break;
-      case GBP_CIC: st = run_scheme<GBP_CIC, 2, 0>(q); break;
-      case GBP_TSC: st = run_scheme<GBP_TSC, 2, 0>(q); break;
-      default: st = run_scheme<GBP_PCS, 2, 0>(q); break;
-    }
-  }
+extern "C" int gbp_deposit_job(const gbp_job* job, int64_t capacity, int N, int mas, int interlace,
+                               float* mesh_out, gbp_deposit_stats* stats_out, void* workspace, size_t ws_bytes,
+                               gbp_stream_t stream_) {
+  DepLayout L;
+  const int st = deposit_layout(capacity, N, mas, interlace, GBP_COMPAT_NONE, L);
   if (st) return st;
-  if (stats_out) {
-    stats_kernel<<<1, 256, 0, stream>>>(q.ctr, q.block_stats, L.nblocks, n, compat, G, stats_out);
-    GBP_LAUNCH_CHECK();
-  }
-  return GBP_OK;
+  if (!job || !mesh_out) return GBP_ERR_INVALID;
+  if (!workspace || ws_bytes < L.total) return GBP_ERR_WORKSPACE;
+  DepGeom g{};
+  g.N = N;
+  g.job = job;
+  g.cap = capacity;
+  return deposit_launch(g, L, capacity, mas, interlace ? 2 : 1, GBP_COMPAT_NONE, nullptr, mesh_out, stats_out,
+                        workspace, reinterpret_cast<cudaStream_t>(stream_));
 }

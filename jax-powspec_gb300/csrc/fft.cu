@@ -122,6 +122,7 @@ int run_fft(const float* mesh, float2* spec, int G, const float2* tw, cudaStream
     auto k = fftz_kernel<N, PAIRS>;
     GBP_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const long long blocks = (npen + 2 * PAIRS - 1) / (2 * PAIRS);
+    GBP_TRACE("fft_z", st);
     k<<<(unsigned)blocks, PAIRS * N / 8, smem, st>>>(mesh, spec, npen, tw);
     GBP_LAUNCH_CHECK();
   }
@@ -129,11 +130,14 @@ int run_fft(const float* mesh, float2* spec, int G, const float2* tw, cudaStream
   const size_t smem = (size_t)N * C * sizeof(float2);
   auto kc = fft_cols_kernel<N, C>;
   GBP_CUDA_TRY(cudaFuncSetAttribute(kc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  // y pass: a plane is one x slab of one grid; rows (y) are P apart
-  kc<<<(unsigned)(G * N * nkb), C * N / 8, smem, st>>>(spec, (long long)N * P, P, G * N, nkb, tw);
-  GBP_LAUNCH_CHECK();
+  {  // y pass: a plane is one x slab of one grid; rows (y) are P apart
+    GBP_TRACE("fft_y", st);
+    kc<<<(unsigned)(G * N * nkb), C * N / 8, smem, st>>>(spec, (long long)N * P, P, G * N, nkb, tw);
+    GBP_LAUNCH_CHECK();
+  }
   // x pass: a plane is one y row of one grid; rows (x) are N*P apart
   for (int g = 0; g < G; ++g) {
+    GBP_TRACE("fft_x", st);
     kc<<<(unsigned)(N * nkb), C * N / 8, smem, st>>>(spec + (long long)g * N * N * P, P, (long long)N * P, N,
                                                       nkb, tw);
     GBP_LAUNCH_CHECK();

@@ -18,9 +18,25 @@
     if (e_ != cudaSuccess) { gbp::set_last_cuda_error(e_); return GBP_ERR_CUDA; } \
   } while (0)
 
+#define GBP_TRACE(name, stream) gbp::TraceScope gbp_trace_scope_(name, stream)
+
 namespace gbp {
 
 void set_last_cuda_error(cudaError_t e);
+
+// Records CUDA events around the launches in its scope while tracing is on
+// (gbp_trace_enable); `name` must be a string literal.
+class TraceScope {
+ public:
+  TraceScope(const char* name, cudaStream_t s);
+  ~TraceScope();
+  TraceScope(const TraceScope&) = delete;
+  TraceScope& operator=(const TraceScope&) = delete;
+
+ private:
+  int slot_;
+  cudaStream_t s_;
+};
 
 // Bytes rounded up to a multiple of 256 (keeps every workspace slice aligned).
 inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }

@@ -441,9 +441,16 @@ __global__ void power_reduce_kernel(const float2* __restrict__ part_ff, int C, i
 __global__ void power_normalize_kernel(const double* sums, const long long* nmodes, const double* ksum, int nb,
                                        double norm_delta, double box3, double kf, const double* mass,
                                        const gbp_deposit_stats* stats, int subtract_shot, double* pk_out,
-                                       double* kmean_out) {
+                                       double* kmean_out, const gbp_job* job, int N) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= nb) return;
+  if (job) {                      // box size from the device job descriptor
+    const double box = job->box_size;
+    const double n2 = (double)N * (double)N;
+    norm_delta = (box / n2) * (box / n2) * (box / n2);
+    box3 = box * box * box;
+    kf = 2.0 * M_PI / box;
+  }
   double norm = norm_delta, shot = 0.0;
   if (mass) {
     const double m = mass[0];
@@ -561,9 +568,13 @@ extern "C" int gbp_power(const void* spectrum, int G, int z_pitch, gbp_bins B, i
   GBP_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, L.warps * 32, L.smem));
   g.groups = L.C;
   const int grid = std::max(1, std::min(L.C, sms * std::max(per_sm, 1)));
-  kern<<<grid, L.warps * 32, L.smem, stream>>>(g);
-  GBP_LAUNCH_CHECK();
+  {
+    GBP_TRACE("power_bins", stream);
+    kern<<<grid, L.warps * 32, L.smem, stream>>>(g);
+    GBP_LAUNCH_CHECK();
+  }
   const int wpb = 8;
+  GBP_TRACE("power_reduce", stream);
   power_reduce_kernel<<<(B->nb + wpb - 1) / wpb, wpb * 32, 0, stream>>>(
       part_ff, L.C, L.NV, B->nb, B->nbe, B->d_nmodes, B->d_ksum, sums_out, nmodes_out,
       (ells & GBP_KSUM) ? ksum_out : nullptr);
@@ -580,8 +591,22 @@ extern "C" int gbp_power_normalize(const double* sums, const long long* nmodes, 
   const double norm_delta = (box / n2) * (box / n2) * (box / n2);
   const double box3 = box * box * box;
   const double kf = 2.0 * M_PI / box;
+  GBP_TRACE("power_normalize", stream);
   power_normalize_kernel<<<(nb + 127) / 128, 128, 0, stream>>>(sums, nmodes, ksum, nb, norm_delta, box3, kf, mass,
-                                                               stats, subtract_shot, pk_out, kmean_out);
+                                                               stats, subtract_shot, pk_out, kmean_out, nullptr, N);
+  GBP_LAUNCH_CHECK();
+  return GBP_OK;
+}
+
+extern "C" int gbp_power_normalize_job(const double* sums, const long long* nmodes, const double* ksum, int nb,
+                                       int N, const gbp_job* job, const double* mass,
+                                       const gbp_deposit_stats* stats, int subtract_shot, double* pk_out,
+                                       double* kmean_out, gbp_stream_t stream_) {
+  cudaStream_t stream = reinterpret_cast<cudaStream_t>(stream_);
+  if (!sums || !nmodes || !pk_out || !job || nb < 1 || N < 1) return GBP_ERR_INVALID;
+  GBP_TRACE("power_normalize", stream);
+  power_normalize_kernel<<<(nb + 127) / 128, 128, 0, stream>>>(sums, nmodes, ksum, nb, 0.0, 0.0, 0.0, mass, stats,
+                                                               subtract_shot, pk_out, kmean_out, job, N);
   GBP_LAUNCH_CHECK();
   return GBP_OK;
 }
@@ -695,9 +720,13 @@ extern "C" int gbp_power_noalloc(const void* spectrum, int G, int z_pitch, gbp_b
   GBP_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, L.warps * 32, L.smem));
   g.groups = L.C;
   const int grid = std::max(1, std::min(L.C, sms * std::max(per_sm, 1)));
-  kern<<<grid, L.warps * 32, L.smem, stream>>>(g);
-  GBP_LAUNCH_CHECK();
+  {
+    GBP_TRACE("power_bins", stream);
+    kern<<<grid, L.warps * 32, L.smem, stream>>>(g);
+    GBP_LAUNCH_CHECK();
+  }
   const int wpb = 8;
+  GBP_TRACE("power_reduce", stream);
   power_reduce_kernel<<<(B->nb + wpb - 1) / wpb, wpb * 32, 0, stream>>>(
       part_ff, L.C, L.NV, B->nb, B->nbe, B->d_nmodes, B->d_ksum, sums_out, nmodes_out,
       (ells & GBP_KSUM) ? ksum_out : nullptr);

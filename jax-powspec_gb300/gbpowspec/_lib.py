@@ -47,6 +47,39 @@ class DepositStats(C.Structure):
 
 STATS_BYTES = C.sizeof(DepositStats)
 
+
+class Job(C.Structure):
+    """Mirror of gbp_job (a mock described in device memory)."""
+
+    _fields_ = [
+        ("x", C.c_void_p),
+        ("y", C.c_void_p),
+        ("z", C.c_void_p),
+        ("w", C.c_void_p),
+        ("n", C.c_longlong),
+        ("inv_cell", C.c_float),
+        ("xmin", C.c_float),
+        ("ymin", C.c_float),
+        ("zmin", C.c_float),
+        ("box_size", C.c_double),
+    ]
+
+
+JOB_BYTES = C.sizeof(Job)
+LANE_GRAPH = 1
+
+
+class TraceRecord(C.Structure):
+    """Mirror of gbp_trace_record."""
+
+    _fields_ = [("kernel", C.c_char_p), ("ms", C.c_float)]
+
+
+class LaneOut(C.Structure):
+    """Mirror of gbp_lane_out (device pointers of the per-job output arrays)."""
+
+    _fields_ = [("pk", C.c_void_p), ("kmean", C.c_void_p), ("nmodes", C.c_void_p), ("stats", C.c_void_p)]
+
 _vp, _i, _i64, _f, _d, _sz = C.c_void_p, C.c_int, C.c_int64, C.c_float, C.c_double, C.c_size_t
 
 # (name, restype, argtypes) for every exported entry point
@@ -68,6 +101,16 @@ SIGNATURES = [
     ("gbp_power", _i, [_vp, _i, _i, _vp, _i, _i, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     ("gbp_power_normalize", _i, [_vp, _vp, _vp, _i, _i, _d, _vp, _vp, _i, _vp, _vp, _vp]),
     ("gbp_power_noalloc", _i, [_vp, _i, _i, _vp, _i, _i, _vp, _vp, _vp, _vp, _vp]),
+    ("gbp_deposit_job", _i, [_vp, _i64, _i, _i, _i, _vp, _vp, _vp, _sz, _vp]),
+    ("gbp_power_normalize_job", _i, [_vp, _vp, _vp, _i, _i, _vp, _vp, _vp, _i, _vp, _vp, _vp]),
+    ("gbp_lane_bytes", _i, [_i, _i, _i, _i, _vp, _i64, C.POINTER(_sz)]),
+    ("gbp_lane_create", _i, [_i, _i, _i, _i, _i, _vp, _i64, _i, C.POINTER(_vp)]),
+    ("gbp_lane_info", _i, [_vp, C.POINTER(_sz), C.POINTER(_i), C.POINTER(_i)]),
+    ("gbp_lane_destroy", _i, [_vp]),
+    ("gbp_lane_run", _i, [_vp, _vp, _i, _i, _i, _vp, _vp]),
+    ("gbp_batch_run", _i, [_vp, _i, _vp, _i, _vp, _vp]),
+    ("gbp_trace_enable", _i, [_i]),
+    ("gbp_trace_collect", _i, [_vp, _i, C.POINTER(_i)]),
 ]
 
 _lock = threading.Lock()

@@ -261,3 +261,20 @@ def normalize(ps: PowerSums, *, n_mesh: int, box_size: float, mass: torch.Tensor
                                           float(box_size), _ptr(mass), _ptr(stats), int(subtract_shot),
                                           _ptr(pk_out), _ptr(kmean_out), _stream_of(dev)), "gbp_power_normalize")
     return pk_out, kmean_out
+
+
+# ---------------------------------------------------------------- tracing
+def trace_enable(capacity: int = 8192) -> None:
+    """Start recording CUDA events around every kernel launch of the library."""
+    check(_lib.load().gbp_trace_enable(int(capacity)), "gbp_trace_enable")
+
+
+def trace_collect() -> list:
+    """Stop tracing; [(kernel name, ms)] in launch order (waits for the launches)."""
+    lib = _lib.load()
+    cap = 65536
+    recs = (_lib.TraceRecord * cap)()
+    n = C.c_int(0)
+    check(lib.gbp_trace_collect(C.cast(recs, C.c_void_p), cap, C.byref(n)), "gbp_trace_collect")
+    return [(recs[i].kernel.decode(), float(recs[i].ms)) for i in range(n.value)]
+

@@ -37,6 +37,7 @@ class PkConfig:
     ells: tuple = (0, 2, 4)
     shot_noise: bool = True
     k_edges: tuple | None = None          # h/Mpc; default kF .. kNyq step kF
+    k_edges_kf: tuple | None = None       # edges in units of kF (exact); overrides k_edges
     origin: tuple = (0.0, 0.0, 0.0)
     kmean: bool = True
 
@@ -49,12 +50,16 @@ class PkConfig:
         return _lib.MAS[self.mas.lower()]
 
     def edges(self) -> np.ndarray:
+        if self.k_edges_kf is not None:
+            return (np.asarray(self.k_edges_kf, np.float64) * (2.0 * np.pi / self.box_size)).astype(np.float32)
         if self.k_edges is None:
             return default_kedges(self.n_mesh, self.box_size)
         return np.asarray(self.k_edges, dtype=np.float32)
 
     def kedges_grid(self) -> np.ndarray:
         """Edges in units of kF (float32): the bins' integer thresholds come from these."""
+        if self.k_edges_kf is not None:
+            return np.asarray(self.k_edges_kf, dtype=np.float32)
         kf = np.float32(2.0 * np.pi / self.box_size)
         return (self.edges() / kf).astype(np.float32)
 
