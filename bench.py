@@ -165,6 +165,7 @@ def kernel_bytes(n: int, N: int, G: int) -> dict:
         "fft_x": 16 * Mh,                         # read + write one grid's spectrum
         "cufft_r2c": G * (4 * M + 8 * Mh),
         "power_bins": G * 8 * Mh,                 # read the spectra once
+        "fft_x_bins": G * 8 * Mh,                 # read the z,y-transformed spectra once (x pass + binning)
     }
 
 

@@ -252,6 +252,22 @@ int gbp_power_normalize_job(const double* sums, const long long* nmodes,
                             double* pk_out, double* kmean_out,
                             gbp_stream_t stream);
 
+/* The 3-D FFT fused with the binning (library transform sizes only: power-of
+ * two meshes 64..1024 and a plan made without the cuFFT override).  The z and
+ * y passes write the partial transform to `spectrum` (the buffer
+ * gbp_fft_r2c would fill); the x pass runs inside the binning kernel, so the
+ * full spectrum never reaches HBM.  Same outputs and arguments as
+ * gbp_fft_r2c followed by gbp_power (src/correlations.py:22-48); the sums
+ * agree to float32 round-off (a different, fixed summation order).
+ * GBP_ERR_UNSUPPORTED when the plan uses cuFFT. */
+int gbp_fft_power_workspace_size(gbp_fft_plan plan, gbp_bins bins, int ells,
+                                 size_t* bytes);
+int gbp_fft_power(gbp_fft_plan plan, const float* mesh, void* spectrum,
+                  gbp_bins bins, int mas_order, int ells, const double* mass,
+                  double* sums_out, long long* nmodes_out, double* ksum_out,
+                  void* workspace, size_t workspace_bytes,
+                  gbp_stream_t stream);
+
 /* ---- Lanes: resident per-mock pipelines for batching and serving --------
  * No reference counterpart (the reference computes one mock per call).
  * A lane owns every buffer one mock needs and, with GBP_LANE_GRAPH, a CUDA

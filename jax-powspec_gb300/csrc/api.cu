@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "gbp_bins.h"
+#include "gbp_fft.h"
 #include "gbp_internal.cuh"
 
 namespace gbp {
@@ -18,7 +19,7 @@ static thread_local cudaError_t g_last_cuda = cudaSuccess;
 void set_last_cuda_error(cudaError_t e) { g_last_cuda = e; }
 
 namespace {
-constexpr int LUT_MAX = 4096;
+constexpr int LUT_MAX = 2048;
 
 long long kmax2_of(int N) {
   const long long h = N / 2;
@@ -208,21 +209,6 @@ extern "C" int gbp_bins_info(gbp_bins B, int* nb, int* reach, int32_t* last) {
 // sizes use a cuFFT 3-D R2C plan (batch = grids) with unpadded rows of
 // N/2+1.  Setting GBP_FFT_BACKEND=cufft when the plan is created forces
 // cuFFT (used to cross-check the two).
-namespace gbp {
-bool own_fft_supported(int N);
-int own_fft_pitch(int N);
-int own_fft_twiddles(int N, float2** d_tw);
-int own_fft_r2c(int N, int G, const float* mesh, float2* spec, const float2* tw, cudaStream_t st);
-}  // namespace gbp
-
-struct gbp_fft_plan_s {
-  bool own;
-  cufftHandle h;
-  float2* tw;       // own transform: twiddles exp(-2 pi i e / N)
-  int n, grids, pitch;
-  size_t ws;
-};
-
 extern "C" int gbp_fft_plan_create(int n, int grids, gbp_fft_plan* out, size_t* ws_bytes) {
   if (!out || n < 2 || n > 4096 || grids < 1 || grids > 64) return GBP_ERR_INVALID;
   *out = nullptr;

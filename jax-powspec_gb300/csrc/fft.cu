@@ -6,8 +6,10 @@
 //           z pencils are packed as one complex pencil (a + i b), transformed,
 //           and split into their half spectra A, B (k = 0 .. N/2):
 //             A[k] = (C[k] + conj C[N-k]) / 2,  B[k] = -i (C[k] - conj C[N-k]) / 2
-//   y pass  in place, 8 adjacent kz columns x N rows per CTA
-//   x pass  in place, same with rows N*P apart
+//   y pass  in place, 8 adjacent kz columns x N rows per CTA; the first
+//           stage reads HBM and the last writes it (fft_pass.cuh)
+//   x pass  in place, same with rows N*P apart (the pipeline fuses it with
+//           the binning instead: xbin.cu)
 //
 // The z rows are padded from N/2+1 to P = N/2+8 complex (64-byte multiples)
 // so every 8-column block of the y and x passes is a whole number of 32-byte
@@ -19,6 +21,8 @@
 #include <vector>
 
 #include "fft_core.cuh"
+#include "fft_pass.cuh"
+#include "gbp_fft.h"
 #include "gbp_internal.cuh"
 
 namespace gbp {
@@ -32,6 +36,15 @@ __host__ __device__ constexpr int zpitch(int N) { return N / 2 + 8; }
 
 // ---- z pass ---------------------------------------------------------------
 // PAIRS complex columns (2*PAIRS real pencils) per CTA, NT = PAIRS * N / 8.
+// Consecutive lanes take consecutive z, so the first stage's loads of each
+// pencil are 128-byte coalesced.  Shared memory is column-major, column q
+// holding pair q with one pad slot per 8 rows (position j + j/8): the
+// stride-8 writes of the first stage and the consecutive accesses of the
+// others then fall on distinct banks.  The last stage stays in shared
+// memory, where each half spectrum needs C[k] and C[N-k] together.
+template <int N>
+__device__ __forceinline__ int zpos(int j) { return j + (j >> 3); }
+
 template <int N, int PAIRS>
 __global__ void __launch_bounds__(PAIRS * N / 8)
 fftz_kernel(const float* __restrict__ mesh, float2* __restrict__ out, long long npencils,
@@ -39,86 +52,69 @@ fftz_kernel(const float* __restrict__ mesh, float2* __restrict__ out, long long 
   constexpr int NT = PAIRS * N / 8;
   constexpr int P = zpitch(N);
   constexpr int H = N / 2;
-  extern __shared__ __align__(16) float2 s[];   // [N][PAIRS]
+  constexpr int LD = N + N / 8;                   // padded column length
+  extern __shared__ __align__(16) float2 s[];     // [PAIRS][LD]
   const int tid = threadIdx.x;
   const long long pen0 = (long long)blockIdx.x * 2 * PAIRS;
   const long long left = npencils - pen0;
   const int npen = left < 2 * PAIRS ? (int)left : 2 * PAIRS;
+  const float* base = mesh + pen0 * N;
 
-  // load: lanes walk 2 float4 of one pencil then the next pencil, so each
-  // warp reads 16 pencils x 32 contiguous bytes (whole sectors)
-  for (int idx = tid; idx < 2 * PAIRS * (N / 4); idx += NT) {
-    const int f = (idx >> 1) % (2 * PAIRS);
-    const int i4 = ((idx >> 1) / (2 * PAIRS)) * 2 + (idx & 1);
-    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (f < npen) v = __ldcs(reinterpret_cast<const float4*>(mesh + (pen0 + f) * N) + i4);
-    float* row = reinterpret_cast<float*>(s) + (f & 1);
-    const int c = f >> 1;
-    row[((4 * i4 + 0) * PAIRS + c) * 2] = v.x;
-    row[((4 * i4 + 1) * PAIRS + c) * 2] = v.y;
-    row[((4 * i4 + 2) * PAIRS + c) * 2] = v.z;
-    row[((4 * i4 + 3) * PAIRS + c) * 2] = v.w;
-  }
-  __syncthreads();
-  fft::fft_columns<N, PAIRS, PAIRS, NT>(s, tw, tid);
+  auto gin = [base, npen](int j, int q) {
+    const float a = 2 * q < npen ? __ldcs(base + (2 * q) * N + j) : 0.0f;
+    const float b = 2 * q + 1 < npen ? __ldcs(base + (2 * q + 1) * N + j) : 0.0f;
+    return make_float2(a, b);
+  };
+  auto sin_ = [](int j, int q) { return s[q * LD + zpos<N>(j)]; };
+  auto sout = [](int j, int q, float2 v) { s[q * LD + zpos<N>(j)] = v; };
+  fft::run_stages<N, PAIRS, NT, true, true>(gin, sin_, sout, sout, tw, tid);
 
   // split the packed spectra and write both pencils' rows (padding -> 0)
   for (int idx = tid; idx < PAIRS * P; idx += NT) {
-    const int q = idx % PAIRS, k = idx / PAIRS;
+    const int q = idx / P, k = idx - (idx / P) * P;
     if (2 * q >= npen) continue;
     float2 a = make_float2(0.f, 0.f), b = make_float2(0.f, 0.f);
     if (k <= H) {
-      const float2 c = s[k * PAIRS + q];
-      const float2 m = s[((N - k) & (N - 1)) * PAIRS + q];
+      const float2 c = s[q * LD + zpos<N>(k)];
+      const float2 m = s[q * LD + zpos<N>((N - k) & (N - 1))];
       const float2 cm = make_float2(m.x, -m.y);
       const float2 sum = cadd(c, cm), dif = cmi(csub(c, cm));
       a = make_float2(0.5f * sum.x, 0.5f * sum.y);
       b = make_float2(0.5f * dif.x, 0.5f * dif.y);
     }
-    out[(pen0 + 2 * q) * P + k] = a;
-    if (2 * q + 1 < npen) out[(pen0 + 2 * q + 1) * P + k] = b;
+    __stcs(out + (pen0 + 2 * q) * P + k, a);
+    if (2 * q + 1 < npen) __stcs(out + (pen0 + 2 * q + 1) * P + k, b);
   }
 }
 
 // ---- y and x passes --------------------------------------------------------
-// C columns (adjacent kz) x N rows per CTA, rows `row_stride` complex apart;
-// CTA b covers plane (b / nkb) and kz block (b % nkb) of its grid.
-template <int N, int C>
-__global__ void __launch_bounds__(C * N / 8)
+// 8 adjacent kz columns x N rows per CTA, rows `row_stride` complex apart;
+// CTA b covers plane (b / nkb) and kz block (b % nkb).  N threads: one
+// radix-8 butterfly each per stage; the first stage loads from HBM and the
+// last stores to HBM (fft_pass.cuh), in place.
+template <int N>
+__global__ void __launch_bounds__(N, 2048 / N < 3 ? 2048 / N : 3)
 fft_cols_kernel(float2* __restrict__ data, long long plane_stride, long long row_stride, int nplanes, int nkb,
                 const float2* __restrict__ tw) {
-  constexpr int NT = C * N / 8;
-  extern __shared__ __align__(16) float2 s[];   // [N][C]
-  const int tid = threadIdx.x;
+  extern __shared__ __align__(16) float2 s[];
   const int plane = blockIdx.x / nkb, kb = blockIdx.x % nkb;
   if (plane >= nplanes) return;
-  float2* base = data + plane * plane_stride + kb * C;
-  for (int idx = tid; idx < N * C / 2; idx += NT) {           // float4 = 2 complex
-    const int row = idx / (C / 2), c2 = idx % (C / 2);
-    const float4 v = __ldcs(reinterpret_cast<const float4*>(base + row * row_stride) + c2);
-    reinterpret_cast<float4*>(s)[idx] = v;
-  }
-  __syncthreads();
-  fft::fft_columns<N, C, C, NT>(s, tw, tid);
-  for (int idx = tid; idx < N * C / 2; idx += NT) {
-    const int row = idx / (C / 2), c2 = idx % (C / 2);
-    __stcs(reinterpret_cast<float4*>(base + row * row_stride) + c2, reinterpret_cast<const float4*>(s)[idx]);
-  }
+  float2* base = data + plane * plane_stride + kb * 8;
+  auto gin = [base, row_stride](int j, int col) { return __ldcs(base + j * row_stride + col); };
+  auto gout = [base, row_stride](int j, int col, float2 v) { __stcs(base + j * row_stride + col, v); };
+  fft::col_fft<N, 1, N, false>(s, gin, gout, tw, threadIdx.x);
 }
 
 template <int N>
 constexpr int z_pairs() { return N >= 256 ? 8 : 32768 / (N * 8); }   // >= 256 threads
 template <int N>
-constexpr int col_block() { return N >= 1024 ? 8 : 8; }
-
-template <int N>
-int run_fft(const float* mesh, float2* spec, int G, const float2* tw, cudaStream_t st) {
+int run_fft(const float* mesh, float2* spec, int G, const float2* tw, cudaStream_t st, bool x_pass = true) {
   constexpr int PAIRS = z_pairs<N>();
   constexpr int P = zpitch(N);
-  constexpr int C = col_block<N>();
+  constexpr int C = 8;                    // kz columns per CTA in the y and x passes
   const long long npen = (long long)G * N * N;
   {
-    const size_t smem = (size_t)N * PAIRS * sizeof(float2);
+    const size_t smem = (size_t)PAIRS * (N + N / 8) * sizeof(float2);
     auto k = fftz_kernel<N, PAIRS>;
     GBP_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const long long blocks = (npen + 2 * PAIRS - 1) / (2 * PAIRS);
@@ -127,19 +123,18 @@ int run_fft(const float* mesh, float2* spec, int G, const float2* tw, cudaStream
     GBP_LAUNCH_CHECK();
   }
   const int nkb = P / C;
-  const size_t smem = (size_t)N * C * sizeof(float2);
-  auto kc = fft_cols_kernel<N, C>;
+  const size_t smem = (size_t)fft::ColBlock<N, 1>::SLAB * sizeof(float2);
+  auto kc = fft_cols_kernel<N>;
   GBP_CUDA_TRY(cudaFuncSetAttribute(kc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   {  // y pass: a plane is one x slab of one grid; rows (y) are P apart
     GBP_TRACE("fft_y", st);
-    kc<<<(unsigned)(G * N * nkb), C * N / 8, smem, st>>>(spec, (long long)N * P, P, G * N, nkb, tw);
+    kc<<<(unsigned)(G * N * nkb), N, smem, st>>>(spec, (long long)N * P, P, G * N, nkb, tw);
     GBP_LAUNCH_CHECK();
   }
   // x pass: a plane is one y row of one grid; rows (x) are N*P apart
-  for (int g = 0; g < G; ++g) {
+  for (int g = 0; x_pass && g < G; ++g) {
     GBP_TRACE("fft_x", st);
-    kc<<<(unsigned)(N * nkb), C * N / 8, smem, st>>>(spec + (long long)g * N * N * P, P, (long long)N * P, N,
-                                                      nkb, tw);
+    kc<<<(unsigned)(N * nkb), N, smem, st>>>(spec + (long long)g * N * N * P, P, (long long)N * P, N, nkb, tw);
     GBP_LAUNCH_CHECK();
   }
   return GBP_OK;
@@ -176,6 +171,17 @@ int own_fft_r2c(int N, int G, const float* mesh, float2* spec, const float2* tw,
     case 256: return run_fft<256>(mesh, spec, G, tw, st);
     case 512: return run_fft<512>(mesh, spec, G, tw, st);
     case 1024: return run_fft<1024>(mesh, spec, G, tw, st);
+    default: return GBP_ERR_UNSUPPORTED;
+  }
+}
+
+int own_fft_zy(int N, int G, const float* mesh, float2* spec, const float2* tw, cudaStream_t st) {
+  switch (N) {
+    case 64: return run_fft<64>(mesh, spec, G, tw, st, false);
+    case 128: return run_fft<128>(mesh, spec, G, tw, st, false);
+    case 256: return run_fft<256>(mesh, spec, G, tw, st, false);
+    case 512: return run_fft<512>(mesh, spec, G, tw, st, false);
+    case 1024: return run_fft<1024>(mesh, spec, G, tw, st, false);
     default: return GBP_ERR_UNSUPPORTED;
   }
 }

@@ -1,0 +1,26 @@
+// Internal view of an FFT plan and the library's own three-pass transform
+// (fft.cu), shared by the C entry points (api.cu) and the fused x-pass +
+// binning (xbin.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cufft.h>
+
+#include "gbpowspec.h"
+
+struct gbp_fft_plan_s {
+  bool own;
+  cufftHandle h;
+  float2* tw;       // own transform: twiddles exp(-2 pi i e / N)
+  int n, grids, pitch;
+  size_t ws;
+};
+
+namespace gbp {
+bool own_fft_supported(int N);
+int own_fft_pitch(int N);
+int own_fft_twiddles(int N, float2** d_tw);
+int own_fft_r2c(int N, int G, const float* mesh, float2* spec, const float2* tw, cudaStream_t st);
+// z and y passes only: spec holds the transform over z and y, not yet over x
+int own_fft_zy(int N, int G, const float* mesh, float2* spec, const float2* tw, cudaStream_t st);
+}  // namespace gbp

@@ -6,8 +6,8 @@
 //
 //   lane_begin    copies job table[cursor] into the lane's job slot
 //   deposit       gbp_deposit_job (reads the slot: particles, n, box)
-//   FFT           gbp_fft_r2c
-//   binning       gbp_power
+//   FFT + binning gbp_fft_power (x pass fused with the binning), or
+//                 gbp_fft_r2c + gbp_power when the plan uses cuFFT
 //   normalise     gbp_power_normalize_job (box from the slot)
 //   lane_end      copies P_l, <k>, counts and deposit statistics to the
 //                 caller's per-job arrays at `cursor`, then cursor += stride
@@ -42,6 +42,7 @@ struct gbp_lane_s {
   gbp_bins bins = nullptr;      // borrowed
   gbp_fft_plan plan = nullptr;  // owned
   int pitch = 0;
+  bool fused = false;           // FFT x pass fused with the binning (library transform)
   size_t dep_ws = 0, fft_ws = 0, pow_ws = 0, bytes = 0;
   char* block = nullptr;        // the lane's single device allocation
   float* mesh = nullptr;
@@ -113,6 +114,8 @@ int lane_sizes(int N, int mas, int interlace, int ells, gbp_bins bins, long long
   if (st) return st;
   st = gbp_power_workspace_size(bins, G, s.pitch, ells, &s.pow);
   if (st) return st;
+  size_t fused = 0;
+  if (gbp_fft_power_workspace_size(plan, bins, ells, &fused) == GBP_OK && fused > s.pow) s.pow = fused;
   s.mesh = align256((size_t)G * N * N * N * sizeof(float));
   s.spec = align256((size_t)G * N * N * s.pitch * sizeof(float2));
   const size_t nb = (size_t)bins->nb;
@@ -132,12 +135,19 @@ int lane_sequence(gbp_lane L, cudaStream_t st) {
   const gbp_stream_t s = reinterpret_cast<gbp_stream_t>(st);
   int r = gbp_deposit_job(L->slot, L->cap, L->N, L->mas, L->G == 2, L->mesh, L->stats, L->dws, L->dep_ws, s);
   if (r) return r;
-  r = gbp_fft_r2c(L->plan, L->mesh, L->spec, L->fws, L->fft_ws, s);
-  if (r) return r;
   const double* mass = reinterpret_cast<const double*>(L->stats);   // gbp_deposit_stats starts with mass[2]
-  r = gbp_power(L->spec, L->G, L->pitch, L->bins, L->mas, L->ells, mass, L->sums, L->nmodes,
-                (L->ells & GBP_KSUM) ? L->ksum : nullptr, L->pws, L->pow_ws, s);
-  if (r) return r;
+  double* ksum = (L->ells & GBP_KSUM) ? L->ksum : nullptr;
+  if (L->fused) {
+    r = gbp_fft_power(L->plan, L->mesh, L->spec, L->bins, L->mas, L->ells, mass, L->sums, L->nmodes, ksum, L->pws,
+                      L->pow_ws, s);
+    if (r) return r;
+  } else {
+    r = gbp_fft_r2c(L->plan, L->mesh, L->spec, L->fws, L->fft_ws, s);
+    if (r) return r;
+    r = gbp_power(L->spec, L->G, L->pitch, L->bins, L->mas, L->ells, mass, L->sums, L->nmodes, ksum, L->pws,
+                  L->pow_ws, s);
+    if (r) return r;
+  }
   r = gbp_power_normalize_job(L->sums, L->nmodes, (L->ells & GBP_KSUM) ? L->ksum : nullptr, L->nb, L->N, L->slot,
                               mass, L->stats, L->shot, L->pk, (L->ells & GBP_KSUM) ? L->kmean : nullptr, s);
   if (r) return r;
@@ -249,6 +259,8 @@ extern "C" int gbp_lane_create(int N, int mas, int interlace, int ells, int shot
   st = lane_sizes(N, mas, interlace, ells, bins, capacity, L->plan, s);
   if (st) { lane_free(L); return st; }
   L->pitch = s.pitch;
+  size_t fused_ws = 0;
+  L->fused = gbp_fft_power_workspace_size(L->plan, bins, ells, &fused_ws) == GBP_OK;
   L->dep_ws = s.dep;
   L->pow_ws = s.pow;
   L->bytes = s.total;

@@ -109,6 +109,8 @@ SIGNATURES = [
     ("gbp_lane_destroy", _i, [_vp]),
     ("gbp_lane_run", _i, [_vp, _vp, _i, _i, _i, _vp, _vp]),
     ("gbp_batch_run", _i, [_vp, _i, _vp, _i, _vp, _vp]),
+    ("gbp_fft_power_workspace_size", _i, [_vp, _vp, _i, C.POINTER(_sz)]),
+    ("gbp_fft_power", _i, [_vp, _vp, _vp, _vp, _i, _i, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     ("gbp_trace_enable", _i, [_i]),
     ("gbp_trace_collect", _i, [_vp, _i, C.POINTER(_i)]),
 ]

@@ -248,6 +248,41 @@ def power(spec: torch.Tensor, grids: int, bins: Bins, *, mas_order: int, ells: i
     return out
 
 
+def fft_power_workspace_size(plan: "FFTPlan", bins: Bins, ells: int) -> int | None:
+    """Workspace of the fused FFT + binning, or None when the plan cannot fuse (cuFFT sizes)."""
+    out = C.c_size_t(0)
+    st = _lib.load().gbp_fft_power_workspace_size(plan.handle, bins.handle, int(ells), C.byref(out))
+    if st == _lib.GBP_ERR_UNSUPPORTED:
+        return None
+    check(st, "gbp_fft_power_workspace_size")
+    return out.value
+
+
+def fft_power(plan: "FFTPlan", mesh: torch.Tensor, spec: torch.Tensor, bins: Bins, *, mas_order: int, ells: int,
+              mass: torch.Tensor | None = None, ws: torch.Tensor | None = None, out: PowerSums | None = None) -> PowerSums:
+    """3-D FFT of the meshes fused with the binning (the spectrum buffer is scratch)."""
+    dev = mesh.device
+    n, G = plan.n, plan.grids
+    if mesh.numel() != G * n ** 3 or mesh.dtype != _F32 or not mesh.is_contiguous():
+        raise ValueError("mesh does not match the plan")
+    if spec.numel() * spec.element_size() < plan.spectrum_floats * 4:
+        raise ValueError("spectrum buffer too small")
+    need = fft_power_workspace_size(plan, bins, ells)
+    if need is None:
+        raise ValueError("this plan cannot fuse the FFT with the binning (cuFFT size)")
+    if ws is None or ws.numel() < need:
+        ws = workspace(need, dev)
+    nb = bins.n_bins
+    if out is None:
+        out = PowerSums(torch.empty((nb, 3), dtype=torch.float64, device=dev),
+                        torch.empty(nb, dtype=torch.int64, device=dev),
+                        torch.empty(nb, dtype=torch.float64, device=dev) if ells & _lib.KSUM else None)
+    check(_lib.load().gbp_fft_power(plan.handle, _ptr(mesh), _ptr(spec), bins.handle, int(mas_order), int(ells),
+                                    _ptr(mass), _ptr(out.sums), _ptr(out.nmodes), _ptr(out.ksum), _ptr(ws),
+                                    ws.numel(), _stream_of(dev)), "gbp_fft_power")
+    return out
+
+
 def normalize(ps: PowerSums, *, n_mesh: int, box_size: float, mass: torch.Tensor | None = None,
               stats: torch.Tensor | None = None, subtract_shot: bool = False,
               pk_out: torch.Tensor | None = None, kmean_out: torch.Tensor | None = None):

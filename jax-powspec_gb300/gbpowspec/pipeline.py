@@ -1,12 +1,13 @@
-"""Fused particle -> P_l(k) pipeline (deposit -> cuFFT R2C -> fused binning).
+"""Fused particle -> P_l(k) pipeline (deposit -> FFT -> fused binning).
 
 ``PowerSpectrum`` keeps every buffer it needs (meshes, spectra, workspaces,
-the cuFFT plan and the bin plan) resident on the device, so repeated calls
+the FFT plan and the bin plan) resident on the device, so repeated calls
 allocate nothing and launch only the kernels:
 
     deposit (count, scan, scatter, tile deposit, stats)  -> gbp_deposit
-    3-D real-to-complex FFT of the G meshes (one plan)    -> gbp_fft_r2c
-    window / interlace / |d|^2 L_l / binning / fold      -> gbp_power
+    3-D FFT, its x pass fused with window / interlace /
+    |d|^2 L_l / binning / fold                            -> gbp_fft_power
+    (cuFFT mesh sizes: gbp_fft_r2c, then gbp_power)
     normalisation, shot noise                             -> gbp_power_normalize
 
 Unlike the reference pipeline (cic_mas_vec -> delta/mean - 1 -> powspec_vec),
@@ -122,7 +123,10 @@ class PowerSpectrum:
                                       torch.empty(nb, dtype=torch.float64, device=dev) if cfg.kmean else None)
         self.pk = torch.empty((nb, 3), dtype=torch.float64, device=dev)
         self.kmean = torch.empty(nb, dtype=torch.float64, device=dev) if cfg.kmean else None
-        self.pow_ws = _native.workspace(_native.power_workspace_size(self.bins, G, self.ells, self.plan.pitch), dev)
+        fused = _native.fft_power_workspace_size(self.plan, self.bins, self.ells)
+        self.fused = fused is not None           # x pass of the FFT fused with the binning
+        pw = fused if self.fused else _native.power_workspace_size(self.bins, G, self.ells, self.plan.pitch)
+        self.pow_ws = _native.workspace(pw, dev)
         self.dep_ws = None
         edges = cfg.edges()
         self.k_edges = edges
@@ -147,11 +151,14 @@ class PowerSpectrum:
         _native.deposit(x, y, z, w, n_mesh=N, inv_cell=np.float32(N / cfg.box_size), origin=cfg.origin,
                         mas=cfg.mas_order, interlace=cfg.interlace, compat=_lib.COMPAT_NONE, wrap=True,
                         out=self.mesh, stats=self.stats, ws=self._dep_ws(n))
-        self.plan.execute(self.mesh, self.spec, self.fft_ws)
         mass = self.stats  # gbp_deposit_stats starts with double mass[2]
-        _native.power(self.spec, cfg.grids, self.bins, mas_order=cfg.mas_order, ells=self.ells,
-                      z_pitch=self.plan.pitch, mass=mass,
-                      ws=self.pow_ws, out=self.sums)
+        if self.fused:
+            _native.fft_power(self.plan, self.mesh, self.spec, self.bins, mas_order=cfg.mas_order, ells=self.ells,
+                              mass=mass, ws=self.pow_ws, out=self.sums)
+        else:
+            self.plan.execute(self.mesh, self.spec, self.fft_ws)
+            _native.power(self.spec, cfg.grids, self.bins, mas_order=cfg.mas_order, ells=self.ells,
+                          z_pitch=self.plan.pitch, mass=mass, ws=self.pow_ws, out=self.sums)
         _native.normalize(self.sums, n_mesh=N, box_size=cfg.box_size, mass=mass, stats=self.stats,
                           subtract_shot=cfg.shot_noise, pk_out=self.pk, kmean_out=self.kmean)
         return PkResult(self.k_edges, self.k_centres, self.kmean, self.pk, self.sums.nmodes, self.stats)
