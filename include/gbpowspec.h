@@ -268,6 +268,36 @@ int gbp_fft_power(gbp_fft_plan plan, const float* mesh, void* spectrum,
                   void* workspace, size_t workspace_bytes,
                   gbp_stream_t stream);
 
+/* Particles -> multipole sums in one call, the deposit fused with the z pass
+ * of the FFT (library transform sizes: power-of-two meshes 64..1024 and a
+ * plan made without the cuFFT override; B-spline deposits).  The mesh is
+ * never written: each column tile of pencils is deposited in shared memory
+ * and transformed along z there; then the y pass and the x pass fused with
+ * the binning.  Interlacing follows the plan (2 grids = interlaced).
+ * Outputs as gbp_deposit (stats_out, required: it carries the mass the
+ * binning and the normalisation use) followed by gbp_fft_power; `spectrum`
+ * is scratch of the plan's spectrum size.  Replaces src/mas.py:88-153 +
+ * src/correlations.py:7-56 for the production path. */
+int gbp_particles_power_workspace_size(int64_t n_particles, gbp_fft_plan plan,
+                                       gbp_bins bins, int mas, int ells,
+                                       size_t* bytes);
+int gbp_particles_power(const float* x, const float* y, const float* z,
+                        const float* w, int64_t n_particles, float xmin,
+                        float ymin, float zmin, float inv_cell,
+                        gbp_fft_plan plan, gbp_bins bins, int mas, int ells,
+                        void* spectrum, double* sums_out, long long* nmodes_out,
+                        double* ksum_out, gbp_deposit_stats* stats_out,
+                        void* workspace, size_t workspace_bytes,
+                        gbp_stream_t stream);
+/* The same for a mock held in a device gbp_job; launch sizes and the
+ * workspace depend only on `capacity`. */
+int gbp_particles_power_job(const gbp_job* job, int64_t capacity,
+                            gbp_fft_plan plan, gbp_bins bins, int mas, int ells,
+                            void* spectrum, double* sums_out,
+                            long long* nmodes_out, double* ksum_out,
+                            gbp_deposit_stats* stats_out, void* workspace,
+                            size_t workspace_bytes, gbp_stream_t stream);
+
 /* ---- Lanes: resident per-mock pipelines for batching and serving --------
  * No reference counterpart (the reference computes one mock per call).
  * A lane owns every buffer one mock needs and, with GBP_LANE_GRAPH, a CUDA

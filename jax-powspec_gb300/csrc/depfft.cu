@@ -1,0 +1,306 @@
+// Particles -> multipole sums with the deposit fused into the z pass of the
+// FFT (library transform sizes: power-of-two meshes 64..1024, B-spline
+// deposits).
+//
+// The mesh is never written.  Particles are bucketed (deposit_core.cuh) by
+// column tile: TX x TY pencils (4 x 4; 2 x 4 at 1024^3) spanning the whole z
+// axis, so a stencil is replicated across x and y tile faces only.  One CTA
+// per column tile and grid:
+//
+//   1. accumulates its bucket in shared memory as exact int64 fixed point
+//      (a native 32-bit atomic on the low word plus a carry into the high
+//      word, as the mesh deposit does),
+//   2. transforms its pencils along z: the first radix-8 stage reads the
+//      integer cells of two pencils (packed as one complex pencil), converts
+//      them to float and writes the complex buffer that aliases the
+//      accumulators; the remaining stages run in place (fft_pass.cuh),
+//   3. splits each packed spectrum into its two real-input half spectra and
+//      writes the pencils' rows of the z-transformed spectrum (P = N/2 + 8
+//      complex per row, as the library's own transform),
+//   4. adds up the tile's exact integer total (the mean density) on the way.
+//
+// Then the y pass (fft.cu) and the x pass fused with the binning (xbin.cu)
+// finish the transform and the P_l sums.  HBM traffic per grid: the
+// spectrum is written once here, read and written by the y pass, and read
+// once by the binning; no mesh goes through HBM.
+#include "deposit_core.cuh"
+#include "fft_pass.cuh"
+#include "gbp_bins.h"
+#include "gbp_fft.h"
+
+namespace gbp {
+namespace {
+
+template <int N>
+struct ColTile {
+  static constexpr int TX = N >= 1024 ? 2 : 4;
+  static constexpr int TY = 4;
+  static constexpr int NPEN = TX * TY;            // pencils per tile; pencil f = lx * TY + ly
+  static constexpr int PAIRS = NPEN / 2;          // complex transforms (pencils 2q, 2q+1)
+  static constexpr int NFFT = PAIRS * N / 8;      // radix-8 butterflies per stage
+  static constexpr int NT = NFFT < 256 ? 256 : NFFT;
+  static constexpr size_t SMEM = (size_t)NPEN * N * 2 * sizeof(unsigned);   // low + high words
+};
+
+template <int N, int MAS, int G>
+__global__ void __launch_bounds__(ColTile<N>::NT, ColTile<N>::NT >= 512 ? 3 : 2)
+deposit_fftz_kernel(DepGeom g, const float4* __restrict__ entries, const unsigned* __restrict__ counts,
+                    const unsigned* __restrict__ cursors, const DepCounters* ctr, const float2* __restrict__ tw,
+                    float2* __restrict__ spec, long long* __restrict__ tile_mass) {
+  using CT = ColTile<N>;
+  constexpr int R = MAS, TX = CT::TX, TY = CT::TY, NPEN = CT::NPEN, PAIRS = CT::PAIRS, NT = CT::NT;
+  constexpr int P = N / 2 + 8, H = N / 2;
+  extern __shared__ __align__(16) unsigned acc32[];
+  unsigned* lo = acc32;                                // [NPEN][N] low words
+  unsigned* hi = acc32 + NPEN * N;                     // [NPEN][N] high words
+  float2* cs = reinterpret_cast<float2*>(acc32);       // [PAIRS][N] complex, aliases the low words
+  __shared__ long long s_part[NT / 32];
+  const int tid = threadIdx.x;
+  const int t = blockIdx.x;
+  const int ty = t % g.nt[1], tx = t / g.nt[1];
+  const int x0 = tx * TX, y0 = ty * TY;
+  const unsigned end = cursors[t];
+  const unsigned beg = end - counts[t];
+  const int s = fixed_scale_exp(ctr->maxw_bits, 0);
+  const float sc = ldexpf(1.0f, s);
+  const float inv_sc = ldexpf(1.0f, -s);
+  const long long gstride = (long long)N * N * P;
+
+  for (int grid = 0; grid < G; ++grid) {
+    {
+      uint4* a4 = reinterpret_cast<uint4*>(acc32);
+      for (int k = tid; k < 2 * NPEN * N / 4; k += NT) a4[k] = make_uint4(0u, 0u, 0u, 0u);
+    }
+    __syncthreads();
+    for (unsigned i = beg + tid; i < end; i += NT) {
+      const float4 e = entries[i];
+      Axis<R> ax, ay, az;
+      make_axis<MAS, 0>(g, e.x, grid, ax);
+      make_axis<MAS, 0>(g, e.y, grid, ay);
+      make_axis<MAS, 0>(g, e.z, grid, az);
+      int lx[R], ly[R], zz[R];
+      local_nodes<R>(ax, N, x0, TX, lx);
+      local_nodes<R>(ay, N, y0, TY, ly);
+      const float wsc = __fmul_rn(e.w, sc);                 // exact: sc is a power of two
+      float wz[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        zz[r] = wrapn(az.first + r, N);
+        wz[r] = __fmul_rn(az.w[r], wsc);
+      }
+#pragma unroll
+      for (int rx = 0; rx < R; ++rx) {
+        if (lx[rx] < 0) continue;
+#pragma unroll
+        for (int ry = 0; ry < R; ++ry) {
+          if (ly[ry] < 0) continue;
+          const float wxy = __fmul_rn(ax.w[rx], ay.w[ry]);
+          const int row = (lx[rx] * TY + ly[ry]) * N;
+          int q[R];
+          unsigned old[R];
+#pragma unroll
+          for (int rz = 0; rz < R; ++rz) {                 // the pencil's low-word adds together
+            q[rz] = __float2int_rn(__fmul_rn(wxy, wz[rz]));
+            old[rz] = atomicAdd(&lo[row + zz[rz]], static_cast<unsigned>(q[rz]));
+          }
+#pragma unroll
+          for (int rz = 0; rz < R; ++rz) {                 // then the carries into the high words
+            const unsigned add = static_cast<unsigned>(q[rz]);
+            const int dh = (q[rz] < 0 ? -1 : 0) + (old[rz] + add < old[rz] ? 1 : 0);
+            if (dh) atomicAdd(&hi[row + zz[rz]], static_cast<unsigned>(dh));
+          }
+        }
+      }
+    }
+    __syncthreads();
+
+    // z transform: pencils 2q and 2q+1 are the real and imaginary parts of column q
+    long long part = 0;
+    auto gin = [&part, inv_sc, lo, hi](int j, int q) {
+      const int c0 = (2 * q) * N + j, c1 = c0 + N;
+      const long long a = (long long)(((unsigned long long)hi[c0] << 32) | lo[c0]);
+      const long long b = (long long)(((unsigned long long)hi[c1] << 32) | lo[c1]);
+      part += a + b;
+      return make_float2(fixed_to_float(a, inv_sc), fixed_to_float(b, inv_sc));
+    };
+    auto sin_ = [cs](int j, int q) { return cs[q * N + fft::zsw(j)]; };
+    auto sout = [cs](int j, int q, float2 v) { cs[q * N + fft::zsw(j)] = v; };
+    fft::run_stages<N, PAIRS, NT, true, true, true>(gin, sin_, sout, sout, tw, tid);
+
+    // split the packed spectra; write all pencils' rows (row padding -> 0)
+    float2* out = spec + grid * gstride;
+    for (int idx = tid; idx < PAIRS * P; idx += NT) {
+      const int q = idx / P, k = idx - (idx / P) * P;
+      float2 a = make_float2(0.f, 0.f), b = make_float2(0.f, 0.f);
+      if (k <= H) {
+        const float2 c = cs[q * N + fft::zsw(k)];
+        const float2 m = cs[q * N + fft::zsw((N - k) & (N - 1))];
+        const float2 cm = make_float2(m.x, -m.y);
+        const float2 sum = fft::cadd(c, cm), dif = fft::cmi(fft::csub(c, cm));
+        a = make_float2(0.5f * sum.x, 0.5f * sum.y);
+        b = make_float2(0.5f * dif.x, 0.5f * dif.y);
+      }
+      const int f0 = 2 * q, f1 = 2 * q + 1;
+      const long long r0 = (long long)(x0 + f0 / TY) * N + (y0 + f0 % TY);
+      const long long r1 = (long long)(x0 + f1 / TY) * N + (y0 + f1 % TY);
+      __stcs(out + r0 * P + k, a);
+      __stcs(out + r1 * P + k, b);
+    }
+
+    // this tile's exact total (read by stats_kernel)
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    if ((tid & 31) == 0) s_part[tid >> 5] = part;
+    __syncthreads();                                   // also: the next grid reuses the accumulators
+    if (tid == 0) {
+      long long tm = 0;
+      for (int k = 0; k < NT / 32; ++k) tm += s_part[k];
+      tile_mass[(long long)grid * gridDim.x + t] = tm;
+    }
+  }
+}
+
+template <int N>
+void tile_shape(int (&tile)[3]) {
+  tile[0] = ColTile<N>::TX;
+  tile[1] = ColTile<N>::TY;
+  tile[2] = N;
+}
+
+int column_tiles(int N, int (&tile)[3]) {
+  switch (N) {
+    case 64: tile_shape<64>(tile); return GBP_OK;
+    case 128: tile_shape<128>(tile); return GBP_OK;
+    case 256: tile_shape<256>(tile); return GBP_OK;
+    case 512: tile_shape<512>(tile); return GBP_OK;
+    case 1024: tile_shape<1024>(tile); return GBP_OK;
+    default: return GBP_ERR_UNSUPPORTED;
+  }
+}
+
+struct PartLayout {
+  DepLayout dep;
+  size_t xbin, total;
+};
+
+int particles_layout(int64_t n, gbp_fft_plan plan, gbp_bins B, int mas, int ells, PartLayout& L) {
+  if (!plan || !B || plan->n != B->N) return GBP_ERR_INVALID;
+  if (!plan->own || (plan->grids != 1 && plan->grids != 2)) return GBP_ERR_UNSUPPORTED;
+  int tile[3];
+  int st = column_tiles(B->N, tile);
+  if (st) return st;
+  st = deposit_layout(n, B->N, mas, plan->grids == 2, GBP_COMPAT_NONE, tile, L.dep);
+  if (st) return st;
+  st = xbin_power_workspace(plan, B, ells, &L.xbin);
+  if (st) return st;
+  L.total = align256(L.dep.total) + L.xbin;
+  return GBP_OK;
+}
+
+template <int N, int MAS, int G>
+int run_fused(const DepGeom& g, const DepLayout& L, const DepBuffers& b, const float2* tw, float2* spec,
+              cudaStream_t st) {
+  int r = bucket_particles<MAS, G, 0>(g, L, b, st);
+  if (r) return r;
+  auto k = deposit_fftz_kernel<N, MAS, G>;
+  const size_t smem = ColTile<N>::SMEM;
+  GBP_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  GBP_TRACE("deposit_fft_z", st);
+  k<<<L.ntiles, ColTile<N>::NT, smem, st>>>(g, b.entries, b.counts, b.cursors, b.ctr, tw, spec, b.tile_mass);
+  GBP_LAUNCH_CHECK();
+  return GBP_OK;
+}
+
+template <int N>
+int dispatch_fused(int mas, int G, const DepGeom& g, const DepLayout& L, const DepBuffers& b, const float2* tw,
+                   float2* spec, cudaStream_t st) {
+  if (G == 2) {
+    switch (mas) {
+      case GBP_NGP: return run_fused<N, GBP_NGP, 2>(g, L, b, tw, spec, st);
+      case GBP_CIC: return run_fused<N, GBP_CIC, 2>(g, L, b, tw, spec, st);
+      case GBP_TSC: return run_fused<N, GBP_TSC, 2>(g, L, b, tw, spec, st);
+      default: return run_fused<N, GBP_PCS, 2>(g, L, b, tw, spec, st);
+    }
+  }
+  switch (mas) {
+    case GBP_NGP: return run_fused<N, GBP_NGP, 1>(g, L, b, tw, spec, st);
+    case GBP_CIC: return run_fused<N, GBP_CIC, 1>(g, L, b, tw, spec, st);
+    case GBP_TSC: return run_fused<N, GBP_TSC, 1>(g, L, b, tw, spec, st);
+    default: return run_fused<N, GBP_PCS, 1>(g, L, b, tw, spec, st);
+  }
+}
+
+int particles_power(DepGeom g, int64_t n_launch, gbp_fft_plan plan, gbp_bins B, int mas, int ells, void* spectrum,
+                    double* sums_out, long long* nmodes_out, double* ksum_out, gbp_deposit_stats* stats_out,
+                    void* workspace, size_t ws_bytes, cudaStream_t st) {
+  if (!spectrum || !sums_out || !nmodes_out || !stats_out) return GBP_ERR_INVALID;
+  if ((reinterpret_cast<uintptr_t>(spectrum) & 15u) != 0) return GBP_ERR_INVALID;
+  PartLayout L;
+  int r = particles_layout(n_launch, plan, B, mas, ells, L);
+  if (r) return r;
+  if (!workspace || ws_bytes < L.total) return GBP_ERR_WORKSPACE;
+  const DepBuffers b = carve_deposit(workspace, L.dep, n_launch);
+  void* xws = static_cast<char*>(workspace) + align256(L.dep.total);
+  for (int a = 0; a < 3; ++a) { g.td[a] = L.dep.td[a]; g.ts[a] = L.dep.ts[a]; g.nt[a] = L.dep.nt[a]; }
+  g.vec_ok = 0;
+  const int N = B->N, G = plan->grids;
+  float2* spec = static_cast<float2*>(spectrum);
+  GBP_CUDA_TRY(cudaMemsetAsync(b.ctr, 0, align256(sizeof(DepCounters)) + align256((size_t)L.dep.ntiles * 4), st));
+  switch (N) {
+    case 64: r = dispatch_fused<64>(mas, G, g, L.dep, b, plan->tw, spec, st); break;
+    case 128: r = dispatch_fused<128>(mas, G, g, L.dep, b, plan->tw, spec, st); break;
+    case 256: r = dispatch_fused<256>(mas, G, g, L.dep, b, plan->tw, spec, st); break;
+    case 512: r = dispatch_fused<512>(mas, G, g, L.dep, b, plan->tw, spec, st); break;
+    default: r = dispatch_fused<1024>(mas, G, g, L.dep, b, plan->tw, spec, st); break;
+  }
+  if (r) return r;
+  r = deposit_stats(b, L.dep, GBP_COMPAT_NONE, G, stats_out, st);
+  if (r) return r;
+  r = own_fft_y(N, G, spec, plan->tw, st);
+  if (r) return r;
+  const double* mass = reinterpret_cast<const double*>(stats_out);   // gbp_deposit_stats starts with mass[2]
+  return xbin_power(plan, spec, B, mas, ells, mass, sums_out, nmodes_out, ksum_out, xws, L.xbin, st);
+}
+
+}  // namespace
+}  // namespace gbp
+
+using namespace gbp;
+
+extern "C" int gbp_particles_power_workspace_size(int64_t n, gbp_fft_plan plan, gbp_bins bins, int mas, int ells,
+                                                  size_t* bytes) {
+  if (!bytes) return GBP_ERR_INVALID;
+  PartLayout L;
+  const int st = particles_layout(n, plan, bins, mas, ells, L);
+  if (st) return st;
+  *bytes = L.total;
+  return GBP_OK;
+}
+
+extern "C" int gbp_particles_power(const float* x, const float* y, const float* z, const float* w, int64_t n,
+                                   float xmin, float ymin, float zmin, float inv_cell, gbp_fft_plan plan,
+                                   gbp_bins bins, int mas, int ells, void* spectrum, double* sums_out,
+                                   long long* nmodes_out, double* ksum_out, gbp_deposit_stats* stats_out,
+                                   void* workspace, size_t ws_bytes, gbp_stream_t stream) {
+  if (n < 0 || (n > 0 && (!x || !y || !z))) return GBP_ERR_INVALID;
+  if (!plan || !bins) return GBP_ERR_INVALID;
+  DepGeom g{};
+  g.x = x; g.y = y; g.z = z; g.w = w; g.n = n;
+  g.ox = xmin; g.oy = ymin; g.oz = zmin; g.inv_cell = inv_cell;
+  g.N = bins->N;
+  g.job = nullptr;
+  return particles_power(g, n, plan, bins, mas, ells, spectrum, sums_out, nmodes_out, ksum_out, stats_out, workspace,
+                         ws_bytes, reinterpret_cast<cudaStream_t>(stream));
+}
+
+extern "C" int gbp_particles_power_job(const gbp_job* job, int64_t capacity, gbp_fft_plan plan, gbp_bins bins,
+                                       int mas, int ells, void* spectrum, double* sums_out, long long* nmodes_out,
+                                       double* ksum_out, gbp_deposit_stats* stats_out, void* workspace,
+                                       size_t ws_bytes, gbp_stream_t stream) {
+  if (!job || capacity < 0 || !plan || !bins) return GBP_ERR_INVALID;
+  DepGeom g{};
+  g.N = bins->N;
+  g.job = job;
+  g.cap = capacity;
+  return particles_power(g, capacity, plan, bins, mas, ells, spectrum, sums_out, nmodes_out, ksum_out, stats_out,
+                         workspace, ws_bytes, reinterpret_cast<cudaStream_t>(stream));
+}

@@ -22,356 +22,10 @@
 // used.  Every cell is written once (zeros included): no clearing pass.
 // The scheme (MAS order, number of grids, reference-compat variant) is a
 // template parameter so every stencil lives in registers.
-#include <cub/device/device_scan.cuh>
-
-#include "gbp_internal.cuh"
+#include "deposit_core.cuh"
 
 namespace gbp {
 namespace {
-
-constexpr int TILE = 16;              // tile edge (cells); >= widest stencil (5)
-constexpr int TILE3 = TILE * TILE * TILE;
-constexpr int DEP_THREADS = 256;
-constexpr int CNT_THREADS = 256;
-constexpr int CNT_ITEMS = 2;          // particles per thread in count/scatter
-constexpr float MAX_ABS_U = 1073741824.0f;  // |u| < 2^30 cells, else dropped
-
-struct DepGeom {
-  const float* x;
-  const float* y;
-  const float* z;
-  const float* w;
-  long long n;
-  float ox, oy, oz, inv_cell;
-  int N;
-  int wrap;         // compat modes only
-  int tdim;         // tile edge actually used (min(TILE, N))
-  int tshift;       // log2(tdim) when tdim is a power of two, else -1
-  int nt;           // tiles per axis
-  int vec_ok;       // mesh pointers are 16-byte aligned (float4 tile stores allowed)
-  const gbp_job* job;  // non-null: particles, n and box geometry are read from here
-  long long cap;       // job mode: the capacity the launches were sized for
-};
-
-// Job mode: the particle pointers, count and box geometry come from a
-// gbp_job in device memory (one broadcast load per thread), so the launch
-// parameters do not depend on the mock.
-__device__ __forceinline__ void resolve_job(DepGeom& g) {
-  if (!g.job) return;
-  const gbp_job j = *g.job;
-  g.x = j.x; g.y = j.y; g.z = j.z; g.w = j.w;
-  g.n = j.n < 0 ? 0 : (j.n > g.cap ? g.cap : j.n);   // the buckets hold `cap` particles at most
-  g.ox = j.xmin; g.oy = j.ymin; g.oz = j.zmin; g.inv_cell = j.inv_cell;
-}
-
-// Node index reduced into [0, N).  Stencil nodes lie within a few cells of
-// [0, N); tiny meshes fall back to the general modulo.
-__device__ __forceinline__ int wrapn(int n, int N) {
-  if (N < 8) return pmod(n, N);
-  return n < 0 ? n + N : (n >= N ? n - N : n);
-}
-
-__device__ __forceinline__ int tile_of(const DepGeom& g, int node) {
-  return g.tshift >= 0 ? (node >> g.tshift) : node / g.tdim;
-}
-
-template <int MAS, int CM>
-struct Scheme {
-  static constexpr int R = CM ? 2 : MAS;    // nodes per axis
-};
-
-// One axis of one particle: nodes first .. first+R-1 (not yet wrapped), their
-// weights, and a mask of nodes that are valid scatter indices (only the
-// reference-compat variants ever drop nodes).
-template <int R>
-struct Axis {
-  int first;
-  unsigned vmask;
-  float w[R];
-};
-
-// B-spline of order MAS with nodes at integer grid coordinates (the
-// reference's node convention: node i sits at xmin + i*H).  `half` shifts
-// the particle by +half a cell (the second, interlaced grid).
-template <int MAS>
-__device__ __forceinline__ void axis_bspline(float u, int N, int half, Axis<MAS>& a) {
-  const float fu = floorf(u);
-  float d = __fsub_rn(u, fu);                 // exact, in [0, 1)
-  int i = pmod(__float2int_rz(fu), N);
-  if (half) {
-    d = __fadd_rn(d, 0.5f);
-    if (d >= 1.0f) { d = __fsub_rn(d, 1.0f); i += 1; }
-  }
-  a.vmask = (1u << MAS) - 1u;
-  if constexpr (MAS == GBP_NGP) {
-    a.first = i + (d >= 0.5f ? 1 : 0);
-    a.w[0] = 1.0f;
-  } else if constexpr (MAS == GBP_CIC) {
-    a.first = i;
-    a.w[0] = __fsub_rn(1.0f, d);
-    a.w[1] = d;
-  } else if constexpr (MAS == GBP_TSC) {
-    const int up = d >= 0.5f ? 1 : 0;           // nearest node is i+up
-    const float s = up ? __fsub_rn(d, 1.0f) : d;  // offset from it, [-0.5, 0.5)
-    a.first = i + up - 1;
-    const float l = 0.5f - s, r = 0.5f + s;
-    a.w[0] = 0.5f * l * l;
-    a.w[1] = 0.75f - s * s;
-    a.w[2] = 0.5f * r * r;
-  } else {                                      // PCS (cubic B-spline)
-    const float t = d, m = 1.0f - d;
-    const float c6 = 1.0f / 6.0f;
-    a.first = i - 1;
-    a.w[0] = m * m * m * c6;
-    a.w[1] = (4.0f - 6.0f * t * t + 3.0f * t * t * t) * c6;
-    a.w[2] = (4.0f - 6.0f * m * m + 3.0f * m * m * m) * c6;
-    a.w[3] = t * t * t * c6;
-  }
-}
-
-// The reference CIC along one axis, bit for bit.
-//   CM == GBP_COMPAT_VEC follows src/mas.py:103-140 (cic_mas_vec): truncating
-//     int32 cast (:107), fraction (:111), wrap = floor-mod of ix+1 (:121);
-//     no-wrap zeroes ixp but tests the zeroed value, so the fraction is kept
-//     (:125-126).
-//   CM == GBP_COMPAT_SCAN follows src/mas.py:44-67 (cic_mas): mdx is computed
-//     before the wrap branch (:56); wrap subtracts n once (:24); no-wrap sets
-//     both ixp and the fraction to zero (:34).
-// Then the scatter's index rule: -N <= idx < 0 maps to idx+N, anything else
-// outside [0, N) drops the update (jax .at[].add default mode).
-template <int CM>
-__device__ __forceinline__ void axis_compat(float u, int N, int wrap, Axis<2>& a) {
-  const int ix = __float2int_rz(u);
-  const float d = __fsub_rn(u, __int2float_rn(ix));
-  const float m = __fsub_rn(1.0f, d);
-  int ixp = ix + 1;
-  float dh = d;
-  if (CM == GBP_COMPAT_VEC) {
-    if (wrap) ixp = pmod(ixp + N, N);
-    else if (ixp >= N) ixp = 0;
-  } else {
-    if (wrap) { if (ixp >= N) ixp -= N; }
-    else if (ixp >= N) { ixp = 0; dh = 0.0f; }
-  }
-  const bool lo_ok = ix >= -N && ix < N;
-  const bool hi_ok = ixp >= -N && ixp < N;
-  const int lo = ix < 0 ? ix + N : ix;
-  const int hi = ixp < 0 ? ixp + N : ixp;
-  // When both are valid, hi == lo + 1 (mod N) in every branch above.
-  a.first = lo_ok ? lo : hi - 1;
-  a.vmask = (lo_ok ? 1u : 0u) | (hi_ok ? 2u : 0u);
-  a.w[0] = m;
-  a.w[1] = dh;
-}
-
-template <int MAS, int CM>
-__device__ __forceinline__ void make_axis(const DepGeom& g, float u, int grid, Axis<Scheme<MAS, CM>::R>& a) {
-  if constexpr (CM != 0) axis_compat<CM>(u, g.N, g.wrap, a);
-  else axis_bspline<MAS>(u, g.N, grid, a);
-}
-
-// The particles of one thread in count/scatter: loads issued together.
-struct Batch {
-  float x[CNT_ITEMS], y[CNT_ITEMS], z[CNT_ITEMS], w[CNT_ITEMS];
-  bool in[CNT_ITEMS];
-};
-
-__device__ __forceinline__ void load_batch(const DepGeom& g, Batch& b) {
-  const long long base = (long long)blockIdx.x * CNT_THREADS * CNT_ITEMS + threadIdx.x;
-#pragma unroll
-  for (int k = 0; k < CNT_ITEMS; ++k) {
-    const long long i = base + (long long)k * CNT_THREADS;
-    b.in[k] = i < g.n;
-    if (b.in[k]) {
-      b.x[k] = __ldcs(g.x + i);
-      b.y[k] = __ldcs(g.y + i);
-      b.z[k] = __ldcs(g.z + i);
-      b.w[k] = g.w ? __ldcs(g.w + i) : 1.0f;
-    }
-  }
-}
-
-// Grid coordinate of a particle; false if it must be dropped (non-finite, or
-// so far outside the box that int32 cells would overflow).
-__device__ __forceinline__ bool grid_coords(const DepGeom& g, float x, float y, float z, float u[3]) {
-  u[0] = __fmul_rn(__fsub_rn(x, g.ox), g.inv_cell);
-  u[1] = __fmul_rn(__fsub_rn(y, g.oy), g.inv_cell);
-  u[2] = __fmul_rn(__fsub_rn(z, g.oz), g.inv_cell);
-  return fabsf(u[0]) < MAX_ABS_U && fabsf(u[1]) < MAX_ABS_U && fabsf(u[2]) < MAX_ABS_U;  // false for NaN
-}
-
-// Distinct tiles touched along one axis by the valid nodes of all grids
-// (at most 3 because a stencil spans at most 5 nodes and tiles are wider).
-template <int MAS, int G, int CM>
-__device__ __forceinline__ int axis_tiles(const DepGeom& g, float u, int& t0, int& t1, int& t2) {
-  constexpr int R = Scheme<MAS, CM>::R;
-  constexpr int W = R + (G - 1);
-  Axis<R> a;
-  make_axis<MAS, CM>(g, u, 0, a);
-  int lo = a.first, hi = a.first + R - 1;
-  if constexpr (CM != 0) {
-    if (a.vmask == 0u) return 0;
-    if (!(a.vmask & 1u)) lo += 1;
-    if (!(a.vmask & 2u)) hi -= 1;
-  }
-  if constexpr (G == 2) {
-    Axis<R> b;
-    make_axis<MAS, CM>(g, u, 1, b);
-    hi = b.first + R - 1;                        // b.first is a.first or a.first + 1
-  }
-  int nt = 0;
-  t0 = t1 = t2 = -1;
-#pragma unroll
-  for (int k = 0; k < W; ++k) {
-    if (lo + k > hi) break;
-    const int t = tile_of(g, wrapn(lo + k, g.N));
-    if (t == t0 || t == t1 || t == t2) continue;
-    if (nt == 0) t0 = t; else if (nt == 1) t1 = t; else t2 = t;
-    ++nt;
-  }
-  return nt;
-}
-
-__device__ __forceinline__ int pick3(int k, int a, int b, int c) { return k == 0 ? a : (k == 1 ? b : c); }
-
-__device__ __forceinline__ float warp_max(float v) {
-  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
-  return v;
-}
-
-__device__ __forceinline__ ff warp_ff_sum(ff v) {
-  for (int o = 16; o > 0; o >>= 1) {
-    ff t{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
-    v = ff_add(v, t);
-  }
-  return v;
-}
-
-struct DepCounters {           // zeroed by one memset per call
-  unsigned int maxw_bits;
-  unsigned int pad_[3];
-};
-
-// Pass 1: tile occupancy counts + weight statistics.
-template <int MAS, int G, int CM>
-__global__ void __launch_bounds__(CNT_THREADS)
-count_kernel(DepGeom gp, unsigned* __restrict__ counts, DepCounters* ctr, float4* block_stats,
-             uint2* block_counts) {
-  DepGeom g = gp;
-  resolve_job(g);
-  float maxw = 0.0f;
-  ff sw{0.f, 0.f}, sw2{0.f, 0.f};
-  unsigned kept = 0, bad = 0;
-  Batch bt;
-  load_batch(g, bt);
-#pragma unroll
-  for (int k = 0; k < CNT_ITEMS; ++k) {
-    if (!bt.in[k]) continue;
-    float u[3];
-    const float w = bt.w[k];
-    if (!grid_coords(g, bt.x[k], bt.y[k], bt.z[k], u)) { ++bad; continue; }
-    int x0, x1, x2, y0, y1, y2, z0, z1, z2;
-    const int nx = axis_tiles<MAS, G, CM>(g, u[0], x0, x1, x2);
-    const int ny = axis_tiles<MAS, G, CM>(g, u[1], y0, y1, y2);
-    const int nz = axis_tiles<MAS, G, CM>(g, u[2], z0, z1, z2);
-    if (nx * ny * nz == 0) continue;
-    ++kept;
-    for (int a = 0; a < nx; ++a)
-      for (int b = 0; b < ny; ++b)
-        for (int c = 0; c < nz; ++c)
-          atomicAdd(&counts[(pick3(a, x0, x1, x2) * g.nt + pick3(b, y0, y1, y2)) * g.nt + pick3(c, z0, z1, z2)], 1u);
-    maxw = fmaxf(maxw, fabsf(w));
-    sw = ff_add_f(sw, w);
-    sw2 = ff_add_f(sw2, __fmul_rn(w, w));
-  }
-  // block reductions in a fixed order -> deterministic partials
-  __shared__ float s_max[CNT_THREADS / 32];
-  __shared__ ff s_sw[CNT_THREADS / 32], s_sw2[CNT_THREADS / 32];
-  __shared__ unsigned s_kept, s_bad;
-  if (threadIdx.x == 0) { s_kept = 0; s_bad = 0; }
-  __syncthreads();
-  maxw = warp_max(maxw);
-  sw = warp_ff_sum(sw);
-  sw2 = warp_ff_sum(sw2);
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  if (lane == 0) { s_max[wid] = maxw; s_sw[wid] = sw; s_sw2[wid] = sw2; }
-  if (kept) atomicAdd(&s_kept, kept);
-  if (bad) atomicAdd(&s_bad, bad);
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    float m = 0.f;
-    ff a{0.f, 0.f}, b{0.f, 0.f};
-    for (int k = 0; k < CNT_THREADS / 32; ++k) {
-      m = fmaxf(m, s_max[k]);
-      a = ff_add(a, s_sw[k]);
-      b = ff_add(b, s_sw2[k]);
-    }
-    block_stats[blockIdx.x] = make_float4(a.hi, a.lo, b.hi, b.lo);
-    block_counts[blockIdx.x] = make_uint2(s_kept, s_bad);
-    if (m > 0.f) atomicMax(&ctr->maxw_bits, __float_as_uint(m));
-  }
-}
-
-// Pass 3: append (u_x, u_y, u_z, w) to every touched tile's bucket.
-template <int MAS, int G, int CM>
-__global__ void __launch_bounds__(CNT_THREADS)
-scatter_kernel(DepGeom gp, unsigned* __restrict__ cursors, float4* __restrict__ entries) {
-  DepGeom g = gp;
-  resolve_job(g);
-  Batch bt;
-  load_batch(g, bt);
-#pragma unroll
-  for (int k = 0; k < CNT_ITEMS; ++k) {
-    if (!bt.in[k]) continue;
-    float u[3];
-    const float w = bt.w[k];
-    if (!grid_coords(g, bt.x[k], bt.y[k], bt.z[k], u)) continue;
-    int x0, x1, x2, y0, y1, y2, z0, z1, z2;
-    const int nx = axis_tiles<MAS, G, CM>(g, u[0], x0, x1, x2);
-    const int ny = axis_tiles<MAS, G, CM>(g, u[1], y0, y1, y2);
-    const int nz = axis_tiles<MAS, G, CM>(g, u[2], z0, z1, z2);
-    if (nx * ny * nz == 0) continue;
-    const float4 e = make_float4(u[0], u[1], u[2], w);
-    for (int a = 0; a < nx; ++a)
-      for (int b = 0; b < ny; ++b)
-        for (int c = 0; c < nz; ++c) {
-          const int t = (pick3(a, x0, x1, x2) * g.nt + pick3(b, y0, y1, y2)) * g.nt + pick3(c, z0, z1, z2);
-          entries[atomicAdd(&cursors[t], 1u)] = e;
-        }
-  }
-}
-
-// Fixed-point exponent s: one contribution w * W (|W| <= 1, or <= 8 for the
-// reference CIC, whose fractions can leave [0,1) off the box) is an integer
-// below 2^30 in magnitude, so it fits one 32-bit atomic on the low word; the
-// 64-bit cell sums hold n * 2^30 without overflow for any n < 2^32.
-// Float32 and integer operations only (GB300's FP64 rate is tiny).
-__device__ __forceinline__ int fixed_scale_exp(unsigned maxw_bits, int compat) {
-  const float maxw = __uint_as_float(maxw_bits);
-  if (!(maxw > 0.0f) || !(maxw < 3.0e38f)) return 0;
-  int ew;
-  frexpf(maxw, &ew);                            // maxw < 2^ew
-  const int s = 30 - ew - (compat ? 3 : 0);
-  return s < -100 ? -100 : (s > 100 ? 100 : s);
-}
-
-// int64 fixed-point value -> float32 (two exact 32-bit halves, one rounding in the FMA).
-__device__ __forceinline__ float fixed_to_float(long long q, float inv_sc) {
-  const int hi = (int)(q >> 32);
-  const unsigned lo = (unsigned)(q & 0xffffffffull);
-  const float v = __fmaf_rn(__int2float_rn(hi), 4294967296.0f, __uint2float_rn(lo));
-  return __fmul_rn(v, inv_sc);
-}
-
-// Local (in-tile) coordinate of stencil node r of an axis, or -1.
-template <int R>
-__device__ __forceinline__ void local_nodes(const Axis<R>& a, int N, int t0, int ext, int (&l)[R]) {
-#pragma unroll
-  for (int r = 0; r < R; ++r) {
-    const int c = wrapn(a.first + r, N) - t0;
-    l[r] = (((a.vmask >> r) & 1u) && c >= 0 && c < ext) ? c : -1;
-  }
-}
 
 // Pass 4: one CTA per tile; the grids go one after the other through the
 // same shared memory (more CTAs per SM), re-reading the bucket from L2.
@@ -392,9 +46,9 @@ deposit_kernel(DepGeom g, const float4* __restrict__ entries, const unsigned* __
   unsigned* lo = acc32;
   unsigned* hi = acc32 + TILE3;
   const int t = blockIdx.x;
-  const int tz = t % g.nt, ty = (t / g.nt) % g.nt, tx = t / (g.nt * g.nt);
-  const int x0 = tx * g.tdim, y0 = ty * g.tdim, z0 = tz * g.tdim;
-  const int ex = min(g.tdim, g.N - x0), ey = min(g.tdim, g.N - y0), ez = min(g.tdim, g.N - z0);
+  const int tz = t % g.nt[2], ty = (t / g.nt[2]) % g.nt[1], tx = t / (g.nt[2] * g.nt[1]);
+  const int x0 = tx * g.td[0], y0 = ty * g.td[1], z0 = tz * g.td[2];
+  const int ex = min(g.td[0], g.N - x0), ey = min(g.td[1], g.N - y0), ez = min(g.td[2], g.N - z0);
 
   const unsigned end = cursors[t];
   const unsigned beg = end - counts[t];
@@ -501,159 +155,19 @@ deposit_kernel(DepGeom g, const float4* __restrict__ entries, const unsigned* __
   }
 }
 
-// Pass 5: fold the per-block statistics and the per-tile mass totals into
-// gbp_deposit_stats.  Float partials are folded in a fixed order; integer
-// totals are exact in any order.
-constexpr int STATS_THREADS = 1024;
-__global__ void __launch_bounds__(STATS_THREADS)
-stats_kernel(const DepCounters* ctr, const float4* block_stats, const uint2* block_counts, int nblocks,
-             const long long* tile_mass, int ntiles, int compat, int G, gbp_deposit_stats* out) {
-  __shared__ ff s_a[32], s_b[32];
-  __shared__ long long s_m[2][32], s_c[2][32];
-  ff a{0.f, 0.f}, b{0.f, 0.f};
-  long long kept = 0, bad = 0, m0 = 0, m1 = 0;
-  for (int k = threadIdx.x; k < nblocks; k += blockDim.x) {
-    const float4 v = block_stats[k];
-    a = ff_add(a, ff{v.x, v.y});
-    b = ff_add(b, ff{v.z, v.w});
-    const uint2 c = block_counts[k];
-    kept += c.x;
-    bad += c.y;
-  }
-  for (int k = threadIdx.x; k < ntiles; k += blockDim.x) {
-    m0 += tile_mass[k];
-    if (G == 2) m1 += tile_mass[ntiles + k];
-  }
-  a = warp_ff_sum(a);
-  b = warp_ff_sum(b);
-  for (int o = 16; o > 0; o >>= 1) {
-    kept += __shfl_xor_sync(0xffffffffu, kept, o);
-    bad += __shfl_xor_sync(0xffffffffu, bad, o);
-    m0 += __shfl_xor_sync(0xffffffffu, m0, o);
-    m1 += __shfl_xor_sync(0xffffffffu, m1, o);
-  }
-  const int wid = threadIdx.x >> 5;
-  if ((threadIdx.x & 31) == 0) {
-    s_a[wid] = a; s_b[wid] = b;
-    s_c[0][wid] = kept; s_c[1][wid] = bad;
-    s_m[0][wid] = m0; s_m[1][wid] = m1;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    ff ta{0.f, 0.f}, tb{0.f, 0.f};
-    long long tk = 0, tbad = 0, tm[2] = {0, 0};
-    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
-      ta = ff_add(ta, s_a[k]);
-      tb = ff_add(tb, s_b[k]);
-      tk += s_c[0][k]; tbad += s_c[1][k];
-      tm[0] += s_m[0][k]; tm[1] += s_m[1][k];
-    }
-    const int s = fixed_scale_exp(ctr->maxw_bits, compat);
-    const double inv = ldexp(1.0, -s);
-    for (int grid = 0; grid < 2; ++grid) out->mass[grid] = grid < G ? (double)tm[grid] * inv : 0.0;
-    out->sum_w = (double)ta.hi + (double)ta.lo;
-    out->sum_w2 = (double)tb.hi + (double)tb.lo;
-    out->n_kept = tk;
-    out->n_nonfinite = tbad;
-    out->scale_exp = s;
-    out->pad_ = 0;
-  }
-}
-
-struct DepLayout {
-  int tdim, tshift, nt, ntiles, maxrep, nblocks;
-  size_t scan_bytes;
-  size_t total;
-};
-
-// Largest number of distinct tiles a run of `width` consecutive nodes can
-// touch along one periodic axis (exact, by enumeration).
-int max_tiles_axis(int N, int tdim, int width) {
-  int best = 0;
-  for (int s = 0; s < N; ++s) {
-    int seen[8], ns = 0;
-    for (int r = 0; r < width; ++r) {
-      const int t = ((s + r) % N) / tdim;
-      bool dup = false;
-      for (int k = 0; k < ns; ++k) dup = dup || seen[k] == t;
-      if (!dup && ns < 8) seen[ns++] = t;
-    }
-    best = ns > best ? ns : best;
-  }
-  return best;
-}
-
-int deposit_layout(int64_t n, int N, int mas, int interlace, int compat, DepLayout& L) {
-  if (N < 1 || N > 4096) return GBP_ERR_INVALID;
-  if (n < 0) return GBP_ERR_INVALID;
-  if (mas < GBP_NGP || mas > GBP_PCS) return GBP_ERR_INVALID;
-  if (compat < 0 || compat > GBP_COMPAT_SCAN) return GBP_ERR_INVALID;
-  if (compat && (mas != GBP_CIC || interlace)) return GBP_ERR_INVALID;
-  L.tdim = N < TILE ? N : TILE;
-  L.tshift = (L.tdim & (L.tdim - 1)) == 0 ? __builtin_ctz(L.tdim) : -1;
-  L.nt = (N + L.tdim - 1) / L.tdim;
-  L.ntiles = L.nt * L.nt * L.nt;
-  const int R = compat ? 2 : mas;
-  const int width = R + (interlace ? 1 : 0);
-  const int m = max_tiles_axis(N, L.tdim, width);
-  if (m > 3) return GBP_ERR_UNSUPPORTED;
-  L.maxrep = m * m * m;
-  if ((double)n * L.maxrep >= 4294967295.0) return GBP_ERR_UNSUPPORTED;
-  L.nblocks = (int)((n + (long long)CNT_THREADS * CNT_ITEMS - 1) / ((long long)CNT_THREADS * CNT_ITEMS));
-  L.scan_bytes = 0;
-  cub::DeviceScan::ExclusiveSum(nullptr, L.scan_bytes, (unsigned*)nullptr, (unsigned*)nullptr, L.ntiles);
-  const size_t nbl = (size_t)(L.nblocks > 0 ? L.nblocks : 1);
-  L.total = align256(sizeof(DepCounters)) + align256((size_t)L.ntiles * 4) * 2 + align256(nbl * sizeof(float4)) +
-            align256(nbl * sizeof(uint2)) + align256((size_t)L.ntiles * 2 * sizeof(long long)) +
-            align256((size_t)n * L.maxrep * sizeof(float4) + 16) + align256(L.scan_bytes);
-  return GBP_OK;
-}
-
-struct Launch {
-  DepGeom g;
-  const DepLayout* L;
-  unsigned* counts;
-  unsigned* cursors;
-  DepCounters* ctr;
-  float4* block_stats;
-  uint2* block_counts;
-  long long* tile_mass;
-  float4* entries;
-  void* scan_tmp;
-  const float* mesh_in;
-  float* mesh_out;
-  cudaStream_t stream;
-};
-
 template <int MAS, int G, int CM>
-int run_scheme(const Launch& q) {
-  const DepLayout& L = *q.L;
-  if (L.nblocks > 0) {
-    GBP_TRACE("deposit_count", q.stream);
-    count_kernel<MAS, G, CM><<<L.nblocks, CNT_THREADS, 0, q.stream>>>(q.g, q.counts, q.ctr, q.block_stats,
-                                                                     q.block_counts);
-    GBP_LAUNCH_CHECK();
-  }
-  {
-    GBP_TRACE("deposit_scan", q.stream);
-    size_t scan_bytes = L.scan_bytes;
-    GBP_CUDA_TRY(cub::DeviceScan::ExclusiveSum(q.scan_tmp, scan_bytes, q.counts, q.cursors, L.ntiles, q.stream));
-  }
-  if (L.nblocks > 0) {
-    GBP_TRACE("deposit_scatter", q.stream);
-    scatter_kernel<MAS, G, CM><<<L.nblocks, CNT_THREADS, 0, q.stream>>>(q.g, q.cursors, q.entries);
-    GBP_LAUNCH_CHECK();
-  }
+int run_scheme(const DepGeom& g, const DepLayout& L, const DepBuffers& b, const float* mesh_in, float* mesh_out,
+               cudaStream_t st) {
+  int r = bucket_particles<MAS, G, CM>(g, L, b, st);
+  if (r) return r;
   const size_t smem = (size_t)2 * TILE3 * sizeof(unsigned);   // lo + hi words, one grid
   // more than 48 KB of dynamic shared memory needs the opt-in (cheap, per call)
   GBP_CUDA_TRY(cudaFuncSetAttribute(deposit_kernel<MAS, G, CM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)smem));
-  {
-    GBP_TRACE("deposit_tiles", q.stream);
-    deposit_kernel<MAS, G, CM><<<L.ntiles, DEP_THREADS, smem, q.stream>>>(q.g, q.entries, q.counts, q.cursors,
-                                                                         q.ctr, q.mesh_in, q.mesh_out, q.tile_mass);
-    GBP_LAUNCH_CHECK();
-  }
+  GBP_TRACE("deposit_tiles", st);
+  deposit_kernel<MAS, G, CM><<<L.ntiles, DEP_THREADS, smem, st>>>(g, b.entries, b.counts, b.cursors, b.ctr, mesh_in,
+                                                                 mesh_out, b.tile_mass);
+  GBP_LAUNCH_CHECK();
   return GBP_OK;
 }
 
@@ -661,52 +175,31 @@ int run_scheme(const Launch& q) {
 // `n` sizes the launches (the particle count, or a job's capacity).
 int deposit_launch(DepGeom g, const DepLayout& L, int64_t n, int mas, int G, int compat, const float* mesh_in,
                    float* mesh_out, gbp_deposit_stats* stats_out, void* workspace, cudaStream_t stream) {
-  Carver cv(workspace);
-  Launch q;
-  const int nbl = L.nblocks > 0 ? L.nblocks : 1;
-  q.ctr = cv.take<DepCounters>(1);
-  q.counts = cv.take<unsigned>(L.ntiles);
-  q.cursors = cv.take<unsigned>(L.ntiles);
-  q.block_stats = cv.take<float4>(nbl);
-  q.block_counts = cv.take<uint2>(nbl);
-  q.tile_mass = cv.take<long long>((size_t)L.ntiles * 2);
-  q.entries = cv.take<float4>((size_t)n * L.maxrep + 1);
-  q.scan_tmp = cv.take<char>(L.scan_bytes);
-  q.L = &L;
-  q.mesh_in = mesh_in;
-  q.mesh_out = mesh_out;
-  q.stream = stream;
-  g.tdim = L.tdim; g.tshift = L.tshift; g.nt = L.nt;
+  const DepBuffers b = carve_deposit(workspace, L, n);
+  for (int a = 0; a < 3; ++a) { g.td[a] = L.td[a]; g.ts[a] = L.ts[a]; g.nt[a] = L.nt[a]; }
   g.vec_ok = ((reinterpret_cast<uintptr_t>(mesh_out) | reinterpret_cast<uintptr_t>(mesh_in)) & 15u) == 0;
-  q.g = g;
-
   // counters + tile counts are adjacent: one memset clears both.
-  GBP_CUDA_TRY(cudaMemsetAsync(q.ctr, 0, align256(sizeof(DepCounters)) + align256((size_t)L.ntiles * 4), stream));
+  GBP_CUDA_TRY(cudaMemsetAsync(b.ctr, 0, align256(sizeof(DepCounters)) + align256((size_t)L.ntiles * 4), stream));
   int st;
-  if (compat == GBP_COMPAT_VEC) st = run_scheme<GBP_CIC, 1, GBP_COMPAT_VEC>(q);
-  else if (compat == GBP_COMPAT_SCAN) st = run_scheme<GBP_CIC, 1, GBP_COMPAT_SCAN>(q);
+  if (compat == GBP_COMPAT_VEC) st = run_scheme<GBP_CIC, 1, GBP_COMPAT_VEC>(g, L, b, mesh_in, mesh_out, stream);
+  else if (compat == GBP_COMPAT_SCAN) st = run_scheme<GBP_CIC, 1, GBP_COMPAT_SCAN>(g, L, b, mesh_in, mesh_out, stream);
   else if (G == 1) {
     switch (mas) {
-      case GBP_NGP: st = run_scheme<GBP_NGP, 1, 0>(q); break;
-      case GBP_CIC: st = run_scheme<GBP_CIC, 1, 0>(q); break;
-      case GBP_TSC: st = run_scheme<GBP_TSC, 1, 0>(q); break;
-      default: st = run_scheme<GBP_PCS, 1, 0>(q); break;
+      case GBP_NGP: st = run_scheme<GBP_NGP, 1, 0>(g, L, b, mesh_in, mesh_out, stream); break;
+      case GBP_CIC: st = run_scheme<GBP_CIC, 1, 0>(g, L, b, mesh_in, mesh_out, stream); break;
+      case GBP_TSC: st = run_scheme<GBP_TSC, 1, 0>(g, L, b, mesh_in, mesh_out, stream); break;
+      default: st = run_scheme<GBP_PCS, 1, 0>(g, L, b, mesh_in, mesh_out, stream); break;
     }
   } else {
     switch (mas) {
-      case GBP_NGP: st = run_scheme<GBP_NGP, 2, 0>(q); break;
-      case GBP_CIC: st = run_scheme<GBP_CIC, 2, 0>(q); break;
-      case GBP_TSC: st = run_scheme<GBP_TSC, 2, 0>(q); break;
-      default: st = run_scheme<GBP_PCS, 2, 0>(q); break;
+      case GBP_NGP: st = run_scheme<GBP_NGP, 2, 0>(g, L, b, mesh_in, mesh_out, stream); break;
+      case GBP_CIC: st = run_scheme<GBP_CIC, 2, 0>(g, L, b, mesh_in, mesh_out, stream); break;
+      case GBP_TSC: st = run_scheme<GBP_TSC, 2, 0>(g, L, b, mesh_in, mesh_out, stream); break;
+      default: st = run_scheme<GBP_PCS, 2, 0>(g, L, b, mesh_in, mesh_out, stream); break;
     }
   }
   if (st) return st;
-  if (stats_out) {
-    GBP_TRACE("deposit_stats", stream);
-    stats_kernel<<<1, STATS_THREADS, 0, stream>>>(q.ctr, q.block_stats, q.block_counts, L.nblocks, q.tile_mass,
-                                                  L.ntiles, compat, G, stats_out);
-    GBP_LAUNCH_CHECK();
-  }
+  if (stats_out) return deposit_stats(b, L, compat, G, stats_out, stream);
   return GBP_OK;
 }
 
@@ -719,7 +212,7 @@ extern "C" int gbp_deposit_workspace_size(int64_t n, int N, int mas, int interla
                                           size_t* bytes) {
   if (!bytes) return GBP_ERR_INVALID;
   DepLayout L;
-  const int st = deposit_layout(n, N, mas, interlace, compat, L);
+  const int st = deposit_layout(n, N, mas, interlace, compat, kCubeTiles, L);
   if (st) return st;
   *bytes = L.total;
   return GBP_OK;
@@ -731,7 +224,7 @@ extern "C" int gbp_deposit(const float* x, const float* y, const float* z, const
                            gbp_deposit_stats* stats_out, void* workspace, size_t ws_bytes,
                            gbp_stream_t stream_) {
   DepLayout L;
-  const int st = deposit_layout(n, N, mas, interlace, compat, L);
+  const int st = deposit_layout(n, N, mas, interlace, compat, kCubeTiles, L);
   if (st) return st;
   if (!mesh_out) return GBP_ERR_INVALID;
   if (n > 0 && (!x || !y || !z)) return GBP_ERR_INVALID;
@@ -749,7 +242,7 @@ extern "C" int gbp_deposit_job(const gbp_job* job, int64_t capacity, int N, int 
                                float* mesh_out, gbp_deposit_stats* stats_out, void* workspace, size_t ws_bytes,
                                gbp_stream_t stream_) {
   DepLayout L;
-  const int st = deposit_layout(capacity, N, mas, interlace, GBP_COMPAT_NONE, L);
+  const int st = deposit_layout(capacity, N, mas, interlace, GBP_COMPAT_NONE, kCubeTiles, L);
   if (st) return st;
   if (!job || !mesh_out) return GBP_ERR_INVALID;
   if (!workspace || ws_bytes < L.total) return GBP_ERR_WORKSPACE;

@@ -38,12 +38,10 @@ __host__ __device__ constexpr int zpitch(int N) { return N / 2 + 8; }
 // PAIRS complex columns (2*PAIRS real pencils) per CTA, NT = PAIRS * N / 8.
 // Consecutive lanes take consecutive z, so the first stage's loads of each
 // pencil are 128-byte coalesced.  Shared memory is column-major, column q
-// holding pair q with one pad slot per 8 rows (position j + j/8): the
-// stride-8 writes of the first stage and the consecutive accesses of the
-// others then fall on distinct banks.  The last stage stays in shared
-// memory, where each half spectrum needs C[k] and C[N-k] together.
-template <int N>
-__device__ __forceinline__ int zpos(int j) { return j + (j >> 3); }
+// holding pair q, with row j stored at fft::zsw(j) (conflict-free for every
+// stage).  The last stage stays in shared memory, where each half spectrum
+// needs C[k] and C[N-k] together.
+using fft::zsw;
 
 template <int N, int PAIRS>
 __global__ void __launch_bounds__(PAIRS * N / 8)
@@ -52,7 +50,7 @@ fftz_kernel(const float* __restrict__ mesh, float2* __restrict__ out, long long 
   constexpr int NT = PAIRS * N / 8;
   constexpr int P = zpitch(N);
   constexpr int H = N / 2;
-  constexpr int LD = N + N / 8;                   // padded column length
+  constexpr int LD = N;
   extern __shared__ __align__(16) float2 s[];     // [PAIRS][LD]
   const int tid = threadIdx.x;
   const long long pen0 = (long long)blockIdx.x * 2 * PAIRS;
@@ -65,8 +63,8 @@ fftz_kernel(const float* __restrict__ mesh, float2* __restrict__ out, long long 
     const float b = 2 * q + 1 < npen ? __ldcs(base + (2 * q + 1) * N + j) : 0.0f;
     return make_float2(a, b);
   };
-  auto sin_ = [](int j, int q) { return s[q * LD + zpos<N>(j)]; };
-  auto sout = [](int j, int q, float2 v) { s[q * LD + zpos<N>(j)] = v; };
+  auto sin_ = [](int j, int q) { return s[q * LD + zsw(j)]; };
+  auto sout = [](int j, int q, float2 v) { s[q * LD + zsw(j)] = v; };
   fft::run_stages<N, PAIRS, NT, true, true>(gin, sin_, sout, sout, tw, tid);
 
   // split the packed spectra and write both pencils' rows (padding -> 0)
@@ -75,8 +73,8 @@ fftz_kernel(const float* __restrict__ mesh, float2* __restrict__ out, long long 
     if (2 * q >= npen) continue;
     float2 a = make_float2(0.f, 0.f), b = make_float2(0.f, 0.f);
     if (k <= H) {
-      const float2 c = s[q * LD + zpos<N>(k)];
-      const float2 m = s[q * LD + zpos<N>((N - k) & (N - 1))];
+      const float2 c = s[q * LD + zsw(k)];
+      const float2 m = s[q * LD + zsw((N - k) & (N - 1))];
       const float2 cm = make_float2(m.x, -m.y);
       const float2 sum = cadd(c, cm), dif = cmi(csub(c, cm));
       a = make_float2(0.5f * sum.x, 0.5f * sum.y);
@@ -108,13 +106,14 @@ fft_cols_kernel(float2* __restrict__ data, long long plane_stride, long long row
 template <int N>
 constexpr int z_pairs() { return N >= 256 ? 8 : 32768 / (N * 8); }   // >= 256 threads
 template <int N>
-int run_fft(const float* mesh, float2* spec, int G, const float2* tw, cudaStream_t st, bool x_pass = true) {
+int run_fft(const float* mesh, float2* spec, int G, const float2* tw, cudaStream_t st, bool x_pass = true,
+            bool z_pass = true) {
   constexpr int PAIRS = z_pairs<N>();
   constexpr int P = zpitch(N);
   constexpr int C = 8;                    // kz columns per CTA in the y and x passes
   const long long npen = (long long)G * N * N;
-  {
-    const size_t smem = (size_t)PAIRS * (N + N / 8) * sizeof(float2);
+  if (z_pass) {
+    const size_t smem = (size_t)PAIRS * N * sizeof(float2);
     auto k = fftz_kernel<N, PAIRS>;
     GBP_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const long long blocks = (npen + 2 * PAIRS - 1) / (2 * PAIRS);
@@ -171,6 +170,17 @@ int own_fft_r2c(int N, int G, const float* mesh, float2* spec, const float2* tw,
     case 256: return run_fft<256>(mesh, spec, G, tw, st);
     case 512: return run_fft<512>(mesh, spec, G, tw, st);
     case 1024: return run_fft<1024>(mesh, spec, G, tw, st);
+    default: return GBP_ERR_UNSUPPORTED;
+  }
+}
+
+int own_fft_y(int N, int G, float2* spec, const float2* tw, cudaStream_t st) {
+  switch (N) {
+    case 64: return run_fft<64>(nullptr, spec, G, tw, st, false, false);
+    case 128: return run_fft<128>(nullptr, spec, G, tw, st, false, false);
+    case 256: return run_fft<256>(nullptr, spec, G, tw, st, false, false);
+    case 512: return run_fft<512>(nullptr, spec, G, tw, st, false, false);
+    case 1024: return run_fft<1024>(nullptr, spec, G, tw, st, false, false);
     default: return GBP_ERR_UNSUPPORTED;
   }
 }

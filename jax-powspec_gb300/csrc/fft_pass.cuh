@@ -25,6 +25,13 @@
 namespace gbp {
 namespace fft {
 
+// Row position of element j in a column-major block walked with consecutive
+// lanes on consecutive rows (IFAST stages): bits 4-6 of j are XORed into bits
+// 0-3, which puts the 16 lanes of a half-warp on 16 distinct 8-byte bank slots
+// in every stage (the stride-8 writes of the first stage, the two
+// interleaved runs of the second, the consecutive rows of the others).
+__device__ __forceinline__ int zsw(int j) { return j ^ ((j >> 4) & 7) ^ (((j >> 6) & 1) << 3); }
+
 template <int N, int SLABS>
 struct ColBlock {
   static constexpr int COLS = 8 * SLABS;
@@ -78,14 +85,17 @@ __device__ __forceinline__ void stage_io(In in, Out out, const float2* __restric
 // through shared memory (`sin` / `sout`), the last stage writes `gout`.
 // Starts without a barrier (the caller orders earlier uses of shared
 // memory).  OUT_SHARED: `gout` writes the shared buffer the last stage
-// reads, so it reads everything first and ends with a barrier.
-template <int N, int COLS, int NT, bool IFAST, bool OUT_SHARED, class GIn, class SIn, class SOut, class GOut>
+// reads, so it reads everything first and ends with a barrier.  IN_SHARED:
+// `gin` reads shared memory that the first stage's writes alias, so the
+// first stage, too, reads everything before it writes.
+template <int N, int COLS, int NT, bool IFAST, bool OUT_SHARED, bool IN_SHARED = false, class GIn, class SIn,
+          class SOut, class GOut>
 __device__ __forceinline__ void run_stages(GIn gin, SIn sin_, SOut sout, GOut gout, const float2* __restrict__ tw,
                                            int tid) {
   using RD = Radices<N>;
   static_assert(RD::stages >= 2, "at least two stages");
   if constexpr (RD::tail == 0) {
-    stage_io<N, 8, COLS, NT, false, true, IFAST>(gin, sout, tw, 1, tid);
+    stage_io<N, 8, COLS, NT, IN_SHARED, true, IFAST>(gin, sout, tw, 1, tid);
     int p = 8;
 #pragma unroll
     for (int st = 1; st < RD::n8 - 1; ++st) {
@@ -94,7 +104,7 @@ __device__ __forceinline__ void run_stages(GIn gin, SIn sin_, SOut sout, GOut go
     }
     stage_io<N, 8, COLS, NT, OUT_SHARED, OUT_SHARED, IFAST>(sin_, gout, tw, p, tid);
   } else {
-    stage_io<N, 8, COLS, NT, false, true, IFAST>(gin, sout, tw, 1, tid);
+    stage_io<N, 8, COLS, NT, IN_SHARED, true, IFAST>(gin, sout, tw, 1, tid);
     int p = 8;
 #pragma unroll
     for (int st = 1; st < RD::n8; ++st) {

@@ -23,4 +23,12 @@ int own_fft_twiddles(int N, float2** d_tw);
 int own_fft_r2c(int N, int G, const float* mesh, float2* spec, const float2* tw, cudaStream_t st);
 // z and y passes only: spec holds the transform over z and y, not yet over x
 int own_fft_zy(int N, int G, const float* mesh, float2* spec, const float2* tw, cudaStream_t st);
+// y pass only (spec already transformed over z)
+int own_fft_y(int N, int G, float2* spec, const float2* tw, cudaStream_t st);
+// x pass fused with the binning + the fold into per-bin sums (xbin.cu); spec
+// holds the transform over z and y
+int xbin_power_workspace(gbp_fft_plan plan, gbp_bins bins, int ells, size_t* bytes);
+int xbin_power(gbp_fft_plan plan, float2* spec, gbp_bins bins, int mas_order, int ells, const double* mass,
+               double* sums_out, long long* nmodes_out, double* ksum_out, void* ws, size_t ws_bytes,
+               cudaStream_t st);
 }  // namespace gbp

@@ -5,9 +5,10 @@
 // of the whole launch sequence:
 //
 //   lane_begin    copies job table[cursor] into the lane's job slot
-//   deposit       gbp_deposit_job (reads the slot: particles, n, box)
-//   FFT + binning gbp_fft_power (x pass fused with the binning), or
-//                 gbp_fft_r2c + gbp_power when the plan uses cuFFT
+//   P_l sums      gbp_particles_power_job (reads the slot: particles, n,
+//                 box): deposit fused with the z pass, y pass, x pass fused
+//                 with the binning; or, when the plan uses cuFFT,
+//                 gbp_deposit_job + gbp_fft_r2c + gbp_power
 //   normalise     gbp_power_normalize_job (box from the slot)
 //   lane_end      copies P_l, <k>, counts and deposit statistics to the
 //                 caller's per-job arrays at `cursor`, then cursor += stride
@@ -42,7 +43,7 @@ struct gbp_lane_s {
   gbp_bins bins = nullptr;      // borrowed
   gbp_fft_plan plan = nullptr;  // owned
   int pitch = 0;
-  bool fused = false;           // FFT x pass fused with the binning (library transform)
+  bool particles = false;       // fused particles -> sums call (library transform sizes)
   size_t dep_ws = 0, fft_ws = 0, pow_ws = 0, bytes = 0;
   char* block = nullptr;        // the lane's single device allocation
   float* mesh = nullptr;
@@ -103,20 +104,26 @@ __global__ void lane_end(LaneDesc* d, int nb, const double* pk, const double* km
 struct LaneSizes {
   size_t mesh, spec, dep, fft, pow, small, total;
   int pitch;
+  bool particles;   // the fused particles -> sums call serves this shape
 };
 
 int lane_sizes(int N, int mas, int interlace, int ells, gbp_bins bins, long long cap, gbp_fft_plan plan,
                LaneSizes& s) {
   const int G = interlace ? 2 : 1;
-  int st = gbp_deposit_workspace_size(cap, N, mas, interlace, GBP_COMPAT_NONE, &s.dep);
+  int st = gbp_fft_plan_pitch(plan, &s.pitch);
   if (st) return st;
-  st = gbp_fft_plan_pitch(plan, &s.pitch);
-  if (st) return st;
-  st = gbp_power_workspace_size(bins, G, s.pitch, ells, &s.pow);
-  if (st) return st;
-  size_t fused = 0;
-  if (gbp_fft_power_workspace_size(plan, bins, ells, &fused) == GBP_OK && fused > s.pow) s.pow = fused;
-  s.mesh = align256((size_t)G * N * N * N * sizeof(float));
+  s.particles = gbp_particles_power_workspace_size(cap, plan, bins, mas, ells, &s.pow) == GBP_OK;
+  if (s.particles) {            // one fused call: no mesh, one workspace
+    s.mesh = 0;
+    s.dep = 0;
+    s.fft = 0;
+  } else {
+    st = gbp_deposit_workspace_size(cap, N, mas, interlace, GBP_COMPAT_NONE, &s.dep);
+    if (st) return st;
+    st = gbp_power_workspace_size(bins, G, s.pitch, ells, &s.pow);
+    if (st) return st;
+    s.mesh = align256((size_t)G * N * N * N * sizeof(float));
+  }
   s.spec = align256((size_t)G * N * N * s.pitch * sizeof(float2));
   const size_t nb = (size_t)bins->nb;
   s.small = align256(nb * 3 * 8) * 2 + align256(nb * 8) * 3 + align256(sizeof(gbp_deposit_stats)) +
@@ -133,23 +140,24 @@ int lane_sequence(gbp_lane L, cudaStream_t st) {
     GBP_LAUNCH_CHECK();
   }
   const gbp_stream_t s = reinterpret_cast<gbp_stream_t>(st);
-  int r = gbp_deposit_job(L->slot, L->cap, L->N, L->mas, L->G == 2, L->mesh, L->stats, L->dws, L->dep_ws, s);
-  if (r) return r;
   const double* mass = reinterpret_cast<const double*>(L->stats);   // gbp_deposit_stats starts with mass[2]
   double* ksum = (L->ells & GBP_KSUM) ? L->ksum : nullptr;
-  if (L->fused) {
-    r = gbp_fft_power(L->plan, L->mesh, L->spec, L->bins, L->mas, L->ells, mass, L->sums, L->nmodes, ksum, L->pws,
-                      L->pow_ws, s);
+  int r;
+  if (L->particles) {
+    r = gbp_particles_power_job(L->slot, L->cap, L->plan, L->bins, L->mas, L->ells, L->spec, L->sums, L->nmodes,
+                                ksum, L->stats, L->pws, L->pow_ws, s);
     if (r) return r;
   } else {
+    r = gbp_deposit_job(L->slot, L->cap, L->N, L->mas, L->G == 2, L->mesh, L->stats, L->dws, L->dep_ws, s);
+    if (r) return r;
     r = gbp_fft_r2c(L->plan, L->mesh, L->spec, L->fws, L->fft_ws, s);
     if (r) return r;
     r = gbp_power(L->spec, L->G, L->pitch, L->bins, L->mas, L->ells, mass, L->sums, L->nmodes, ksum, L->pws,
                   L->pow_ws, s);
     if (r) return r;
   }
-  r = gbp_power_normalize_job(L->sums, L->nmodes, (L->ells & GBP_KSUM) ? L->ksum : nullptr, L->nb, L->N, L->slot,
-                              mass, L->stats, L->shot, L->pk, (L->ells & GBP_KSUM) ? L->kmean : nullptr, s);
+  r = gbp_power_normalize_job(L->sums, L->nmodes, ksum, L->nb, L->N, L->slot, mass, L->stats, L->shot, L->pk,
+                              (L->ells & GBP_KSUM) ? L->kmean : nullptr, s);
   if (r) return r;
   GBP_TRACE("lane_end", st);
   lane_end<<<1, 256, 0, st>>>(L->desc, L->nb, L->pk, (L->ells & GBP_KSUM) ? L->kmean : nullptr, L->nmodes,
@@ -259,8 +267,7 @@ extern "C" int gbp_lane_create(int N, int mas, int interlace, int ells, int shot
   st = lane_sizes(N, mas, interlace, ells, bins, capacity, L->plan, s);
   if (st) { lane_free(L); return st; }
   L->pitch = s.pitch;
-  size_t fused_ws = 0;
-  L->fused = gbp_fft_power_workspace_size(L->plan, bins, ells, &fused_ws) == GBP_OK;
+  L->particles = s.particles;
   L->dep_ws = s.dep;
   L->pow_ws = s.pow;
   L->bytes = s.total;

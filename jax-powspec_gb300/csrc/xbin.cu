@@ -40,7 +40,6 @@ namespace gbp {
 namespace {
 
 constexpr int XB_THREADS = 512;
-constexpr int XB_WARPS = XB_THREADS / 32;
 constexpr int XB_BINS = 8;                   // per-warp bin arrays; warps w and w + 8 share one
 constexpr int XB_C = 8;                      // kz columns per work item
 
@@ -292,9 +291,9 @@ int dispatch_xbin(const PowGeom& g, int NV, bool inter, size_t smem, cudaStream_
 }  // namespace
 }  // namespace gbp
 
-using namespace gbp;
+namespace gbp {
 
-extern "C" int gbp_fft_power_workspace_size(gbp_fft_plan plan, gbp_bins B, int ells, size_t* bytes) {
+int xbin_power_workspace(gbp_fft_plan plan, gbp_bins B, int ells, size_t* bytes) {
   if (!plan || !B || !bytes || plan->n != B->N) return GBP_ERR_INVALID;
   if (!plan->own || (plan->grids != 1 && plan->grids != 2)) return GBP_ERR_UNSUPPORTED;
   XbLayout L;
@@ -304,26 +303,21 @@ extern "C" int gbp_fft_power_workspace_size(gbp_fft_plan plan, gbp_bins B, int e
   return GBP_OK;
 }
 
-extern "C" int gbp_fft_power(gbp_fft_plan plan, const float* mesh, void* spectrum, gbp_bins B, int mas_order,
-                             int ells, const double* mass, double* sums_out, long long* nmodes_out, double* ksum_out,
-                             void* workspace, size_t ws_bytes, gbp_stream_t stream_) {
-  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream_);
-  if (!plan || !mesh || !spectrum || !B || !sums_out || !nmodes_out) return GBP_ERR_INVALID;
+int xbin_power(gbp_fft_plan plan, float2* spec, gbp_bins B, int mas_order, int ells, const double* mass,
+               double* sums_out, long long* nmodes_out, double* ksum_out, void* workspace, size_t ws_bytes,
+               cudaStream_t st) {
+  if (!plan || !spec || !B || !sums_out || !nmodes_out) return GBP_ERR_INVALID;
   if (plan->n != B->N) return GBP_ERR_INVALID;
   if (!plan->own || (plan->grids != 1 && plan->grids != 2)) return GBP_ERR_UNSUPPORTED;
   if (mas_order < 0 || mas_order > 8) return GBP_ERR_INVALID;
   if ((ells & (GBP_ELL0 | GBP_ELL2 | GBP_ELL4)) == 0 || (ells & ~15)) return GBP_ERR_INVALID;
   if ((ells & GBP_KSUM) && !ksum_out) return GBP_ERR_INVALID;
-  if (((reinterpret_cast<uintptr_t>(mesh) | reinterpret_cast<uintptr_t>(spectrum)) & 15u) != 0) return GBP_ERR_INVALID;
+  if ((reinterpret_cast<uintptr_t>(spec) & 15u) != 0) return GBP_ERR_INVALID;
   XbLayout L;
   int r = xbin_layout(B, plan->grids, ells, L);
   if (r) return r;
   if (!workspace || ws_bytes < L.ws) return GBP_ERR_WORKSPACE;
   const int N = B->N, G = plan->grids;
-  float2* spec = static_cast<float2*>(spectrum);
-  r = own_fft_zy(N, G, mesh, spec, plan->tw, st);
-  if (r) return r;
-
   PowGeom g{};
   g.s0 = spec;
   g.s1 = G == 2 ? spec + (long long)N * N * plan->pitch : nullptr;
@@ -363,4 +357,30 @@ extern "C" int gbp_fft_power(gbp_fft_plan plan, const float* mesh, void* spectru
       (ells & GBP_KSUM) ? ksum_out : nullptr);
   GBP_LAUNCH_CHECK();
   return GBP_OK;
+}
+
+}  // namespace gbp
+
+using namespace gbp;
+
+extern "C" int gbp_fft_power_workspace_size(gbp_fft_plan plan, gbp_bins B, int ells, size_t* bytes) {
+  return xbin_power_workspace(plan, B, ells, bytes);
+}
+
+extern "C" int gbp_fft_power(gbp_fft_plan plan, const float* mesh, void* spectrum, gbp_bins B, int mas_order,
+                             int ells, const double* mass, double* sums_out, long long* nmodes_out, double* ksum_out,
+                             void* workspace, size_t ws_bytes, gbp_stream_t stream_) {
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream_);
+  if (!plan || !mesh || !spectrum || !B || !sums_out || !nmodes_out) return GBP_ERR_INVALID;
+  if (plan->n != B->N) return GBP_ERR_INVALID;
+  if (!plan->own || (plan->grids != 1 && plan->grids != 2)) return GBP_ERR_UNSUPPORTED;
+  if (((reinterpret_cast<uintptr_t>(mesh) | reinterpret_cast<uintptr_t>(spectrum)) & 15u) != 0) return GBP_ERR_INVALID;
+  size_t need = 0;
+  int r = xbin_power_workspace(plan, B, ells, &need);
+  if (r) return r;
+  if (!workspace || ws_bytes < need) return GBP_ERR_WORKSPACE;
+  float2* spec = static_cast<float2*>(spectrum);
+  r = own_fft_zy(B->N, plan->grids, mesh, spec, plan->tw, st);
+  if (r) return r;
+  return xbin_power(plan, spec, B, mas_order, ells, mass, sums_out, nmodes_out, ksum_out, workspace, ws_bytes, st);
 }

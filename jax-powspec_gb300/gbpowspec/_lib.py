@@ -111,6 +111,10 @@ SIGNATURES = [
     ("gbp_batch_run", _i, [_vp, _i, _vp, _i, _vp, _vp]),
     ("gbp_fft_power_workspace_size", _i, [_vp, _vp, _i, C.POINTER(_sz)]),
     ("gbp_fft_power", _i, [_vp, _vp, _vp, _vp, _i, _i, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
+    ("gbp_particles_power_workspace_size", _i, [_i64, _vp, _vp, _i, _i, C.POINTER(_sz)]),
+    ("gbp_particles_power", _i, [_vp, _vp, _vp, _vp, _i64, _f, _f, _f, _f, _vp, _vp, _i, _i, _vp, _vp, _vp, _vp,
+                                 _vp, _vp, _sz, _vp]),
+    ("gbp_particles_power_job", _i, [_vp, _i64, _vp, _vp, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     ("gbp_trace_enable", _i, [_i]),
     ("gbp_trace_collect", _i, [_vp, _i, C.POINTER(_i)]),
 ]

@@ -283,6 +283,48 @@ def fft_power(plan: "FFTPlan", mesh: torch.Tensor, spec: torch.Tensor, bins: Bin
     return out
 
 
+def particles_power_workspace_size(n: int, plan: "FFTPlan", bins: Bins, mas: int, ells: int) -> int | None:
+    """Workspace of the fused particles -> sums path, or None when the plan cannot fuse (cuFFT sizes)."""
+    out = C.c_size_t(0)
+    st = _lib.load().gbp_particles_power_workspace_size(int(n), plan.handle, bins.handle, int(mas), int(ells),
+                                                         C.byref(out))
+    if st == _lib.GBP_ERR_UNSUPPORTED:
+        return None
+    check(st, "gbp_particles_power_workspace_size")
+    return out.value
+
+
+def particles_power(x: torch.Tensor, y: torch.Tensor, z: torch.Tensor, w: torch.Tensor | None, *, plan: "FFTPlan",
+                    bins: Bins, mas: int, ells: int, inv_cell: float, origin=(0.0, 0.0, 0.0),
+                    spec: torch.Tensor, stats: torch.Tensor, ws: torch.Tensor | None = None,
+                    out: PowerSums | None = None) -> PowerSums:
+    """Deposit fused with the z pass, y pass, x pass fused with the binning (one library call)."""
+    dev = x.device
+    n = x.numel()
+    for t, nm in ((x, "x"), (y, "y"), (z, "z"), (w, "w")):
+        if t is not None and not (t.is_cuda and t.dtype == _F32 and t.is_contiguous() and t.numel() == n
+                                  and t.device == dev):
+            raise ValueError(f"{nm} must be a contiguous float32 CUDA tensor with {n} elements on {dev}")
+    if spec.numel() * spec.element_size() < plan.spectrum_floats * 4:
+        raise ValueError("spectrum buffer too small")
+    need = particles_power_workspace_size(n, plan, bins, mas, ells)
+    if need is None:
+        raise ValueError("this plan cannot fuse the deposit with the FFT (cuFFT size)")
+    if ws is None or ws.numel() < need:
+        ws = workspace(need, dev)
+    nb = bins.n_bins
+    if out is None:
+        out = PowerSums(torch.empty((nb, 3), dtype=torch.float64, device=dev),
+                        torch.empty(nb, dtype=torch.int64, device=dev),
+                        torch.empty(nb, dtype=torch.float64, device=dev) if ells & _lib.KSUM else None)
+    check(_lib.load().gbp_particles_power(
+        _ptr(x), _ptr(y), _ptr(z), _ptr(w), n, float(np.float32(origin[0])), float(np.float32(origin[1])),
+        float(np.float32(origin[2])), float(np.float32(inv_cell)), plan.handle, bins.handle, int(mas), int(ells),
+        _ptr(spec), _ptr(out.sums), _ptr(out.nmodes), _ptr(out.ksum), _ptr(stats), _ptr(ws), ws.numel(),
+        _stream_of(dev)), "gbp_particles_power")
+    return out
+
+
 def normalize(ps: PowerSums, *, n_mesh: int, box_size: float, mass: torch.Tensor | None = None,
               stats: torch.Tensor | None = None, subtract_shot: bool = False,
               pk_out: torch.Tensor | None = None, kmean_out: torch.Tensor | None = None):

@@ -1,13 +1,14 @@
 """Fused particle -> P_l(k) pipeline (deposit -> FFT -> fused binning).
 
-``PowerSpectrum`` keeps every buffer it needs (meshes, spectra, workspaces,
-the FFT plan and the bin plan) resident on the device, so repeated calls
-allocate nothing and launch only the kernels:
+``PowerSpectrum`` keeps every buffer it needs (spectra, workspaces, the FFT
+plan and the bin plan) resident on the device, so repeated calls allocate
+nothing and launch only the kernels:
 
-    deposit (count, scan, scatter, tile deposit, stats)  -> gbp_deposit
-    3-D FFT, its x pass fused with window / interlace /
-    |d|^2 L_l / binning / fold                            -> gbp_fft_power
-    (cuFFT mesh sizes: gbp_fft_r2c, then gbp_power)
+    bucket particles by column tile, deposit each tile
+    and transform it along z in shared memory, y pass,
+    x pass fused with window / interlace / |d|^2 L_l /
+    binning / fold                                        -> gbp_particles_power
+    (cuFFT mesh sizes: gbp_deposit, gbp_fft_r2c, gbp_power)
     normalisation, shot noise                             -> gbp_power_normalize
 
 Unlike the reference pipeline (cic_mas_vec -> delta/mean - 1 -> powspec_vec),
@@ -101,7 +102,14 @@ def algorithmic_bytes(n_particles: int, n_mesh: int, grids: int, weighted: bool 
 
 
 class PowerSpectrum:
-    """Resident pipeline for one configuration on one device."""
+    """Resident pipeline for one configuration on one device.
+
+    Library transform sizes (power-of-two meshes 64..1024) run the fused
+    path, one call to gbp_particles_power: the deposit fused with the z pass
+    of the FFT, the y pass, the x pass fused with the binning; no mesh is
+    stored.  Other sizes deposit a mesh (gbp_deposit), transform it with
+    cuFFT (gbp_fft_r2c) and bin it (gbp_power).
+    """
 
     def __init__(self, cfg: PkConfig, device=None):
         if not torch.cuda.is_available():
@@ -110,11 +118,9 @@ class PowerSpectrum:
         self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
         N, G = cfg.n_mesh, cfg.grids
         dev = self.device
-        self.mesh = torch.empty((G, N, N, N), dtype=torch.float32, device=dev)
         self.stats = torch.empty(_lib.STATS_BYTES, dtype=torch.uint8, device=dev)
         self.plan = _native.fft_plan(N, G, dev)
         self.spec = torch.empty(self.plan.spectrum_floats, dtype=torch.float32, device=dev)
-        self.fft_ws = _native.workspace(self.plan.ws_bytes, dev)
         self.bins = _native.bins_for(cfg.kedges_grid(), N, dev)
         self.ells = cfg.ells_mask()
         nb = self.bins.n_bins
@@ -123,39 +129,47 @@ class PowerSpectrum:
                                       torch.empty(nb, dtype=torch.float64, device=dev) if cfg.kmean else None)
         self.pk = torch.empty((nb, 3), dtype=torch.float64, device=dev)
         self.kmean = torch.empty(nb, dtype=torch.float64, device=dev) if cfg.kmean else None
-        fused = _native.fft_power_workspace_size(self.plan, self.bins, self.ells)
-        self.fused = fused is not None           # x pass of the FFT fused with the binning
-        pw = fused if self.fused else _native.power_workspace_size(self.bins, G, self.ells, self.plan.pitch)
-        self.pow_ws = _native.workspace(pw, dev)
-        self.dep_ws = None
+        # fused path when the library's own transform serves this mesh
+        self.fused = _native.particles_power_workspace_size(1, self.plan, self.bins, cfg.mas_order,
+                                                            self.ells) is not None
+        self.mesh = None if self.fused else torch.empty((G, N, N, N), dtype=torch.float32, device=dev)
+        self.fft_ws = None if self.fused else _native.workspace(self.plan.ws_bytes, dev)
+        self.pow_ws = None if self.fused else _native.workspace(
+            _native.power_workspace_size(self.bins, G, self.ells, self.plan.pitch), dev)
+        self.ws = None
         edges = cfg.edges()
         self.k_edges = edges
         self.k_centres = torch.from_numpy(0.5 * (edges[1:].astype(np.float64) + edges[:-1])).to(dev)
 
-    def _dep_ws(self, n: int) -> torch.Tensor:
+    def _ws(self, n: int) -> torch.Tensor:
         cfg = self.cfg
-        need = _native.deposit_workspace_size(n, cfg.n_mesh, cfg.mas_order, cfg.interlace, _lib.COMPAT_NONE)
-        if self.dep_ws is None or self.dep_ws.numel() < need:
-            self.dep_ws = _native.workspace(int(need * 1.25) + 4096, self.device)
-        return self.dep_ws
+        if self.fused:
+            need = _native.particles_power_workspace_size(n, self.plan, self.bins, cfg.mas_order, self.ells)
+        else:
+            need = _native.deposit_workspace_size(n, cfg.n_mesh, cfg.mas_order, cfg.interlace, _lib.COMPAT_NONE)
+        if self.ws is None or self.ws.numel() < need:
+            self.ws = _native.workspace(int(need * 1.25) + 4096, self.device)
+        return self.ws
 
     def reserve(self, n_particles: int) -> None:
-        """Pre-size the deposit workspace (so a timed or captured call allocates nothing)."""
-        self._dep_ws(int(n_particles))
+        """Pre-size the workspace (so a timed or captured call allocates nothing)."""
+        self._ws(int(n_particles))
 
     def run(self, x: torch.Tensor, y: torch.Tensor, z: torch.Tensor, w: torch.Tensor | None = None) -> PkResult:
         """Enqueue the whole pipeline on the current stream (no host synchronisation)."""
         cfg = self.cfg
         N = cfg.n_mesh
         n = x.numel()
-        _native.deposit(x, y, z, w, n_mesh=N, inv_cell=np.float32(N / cfg.box_size), origin=cfg.origin,
-                        mas=cfg.mas_order, interlace=cfg.interlace, compat=_lib.COMPAT_NONE, wrap=True,
-                        out=self.mesh, stats=self.stats, ws=self._dep_ws(n))
+        inv_cell = np.float32(N / cfg.box_size)
         mass = self.stats  # gbp_deposit_stats starts with double mass[2]
         if self.fused:
-            _native.fft_power(self.plan, self.mesh, self.spec, self.bins, mas_order=cfg.mas_order, ells=self.ells,
-                              mass=mass, ws=self.pow_ws, out=self.sums)
+            _native.particles_power(x, y, z, w, plan=self.plan, bins=self.bins, mas=cfg.mas_order, ells=self.ells,
+                                    inv_cell=inv_cell, origin=cfg.origin, spec=self.spec, stats=self.stats,
+                                    ws=self._ws(n), out=self.sums)
         else:
+            _native.deposit(x, y, z, w, n_mesh=N, inv_cell=inv_cell, origin=cfg.origin, mas=cfg.mas_order,
+                            interlace=cfg.interlace, compat=_lib.COMPAT_NONE, wrap=True, out=self.mesh,
+                            stats=self.stats, ws=self._ws(n))
             self.plan.execute(self.mesh, self.spec, self.fft_ws)
             _native.power(self.spec, cfg.grids, self.bins, mas_order=cfg.mas_order, ells=self.ells,
                           z_pitch=self.plan.pitch, mass=mass, ws=self.pow_ws, out=self.sums)

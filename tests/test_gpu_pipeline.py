@@ -75,11 +75,12 @@ def test_pipeline_is_bitwise_deterministic():
     x, y, z, _ = _cat(200_000, 1000.0, seed=11, grid=64)
     t = [torch.from_numpy(a).cuda() for a in (x, y, z)]
     ps = PowerSpectrum(PkConfig(n_mesh=64, box_size=1000.0, mas="tsc", interlace=True))
+    assert ps.fused
     a = ps.run(*t).pk.clone()
-    mesh_a = ps.mesh.clone()
+    spec_a = ps.spec.clone()                     # the z,y-transformed spectra the binning read
     perm = torch.randperm(t[0].numel(), device="cuda")
     b = ps.run(*(u[perm].contiguous() for u in t)).pk.clone()
-    assert torch.equal(ps.mesh, mesh_a)          # particle order does not matter
+    assert torch.equal(ps.spec, spec_a)          # particle order does not matter
     assert torch.equal(a, b)
 
 
