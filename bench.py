@@ -196,6 +196,105 @@ def trace_breakdown(ps, xd, yd, zd, reps: int, n: int) -> dict:
     return out
 
 
+def covariance_leg(dev, seed: int, n_mocks: int = 256) -> dict:
+    """Batched covariance run: n_mocks lognormal mocks (device generator, a different seed each), particle
+    counts log-uniform in [2e5, 2e6], half on 256^3 and half on 128^3, L = 1500, CIC + interlacing,
+    l = 0, 2; both halves run concurrently; returns throughput and the covariance shapes."""
+    import torch
+    from gbpowspec.batch import BatchRunner, ParticleArena, covariance, run_mixed
+    from gbpowspec.synth import lognormal_catalogue_gpu
+    rng = np.random.default_rng(seed)
+    box = 1500.0
+    counts = np.exp(rng.uniform(np.log(2e5), np.log(2e6), n_mocks)).astype(np.int64)
+    meshes = np.where(np.arange(n_mocks) % 2 == 0, 256, 128)
+    arena = ParticleArena.empty(counts, device=dev)
+    t0 = time.perf_counter()
+    for i in range(n_mocks):
+        lognormal_catalogue_gpu(int(counts[i]), box, grid=int(meshes[i]), seed=int(seed * 100003 + i),
+                                rsd_sigma=3.0, device=dev, out=arena.views(i))
+    torch.cuda.synchronize(dev)
+    t_gen = time.perf_counter() - t0
+    idx = {N: np.nonzero(meshes == N)[0] for N in (256, 128)}
+    jobs = {N: arena.job_table(box, N, indices=idx[N]) for N in idx}
+    cap = int(counts.max())
+    runners = {N: BatchRunner(N, capacity=cap, mas="cic", interlace=True, ells=(0, 2), n_lanes=3, device=dev)
+               for N in idx}
+    run_mixed([(runners[N], jobs[N]) for N in idx])              # warm
+    torch.cuda.synchronize(dev)
+    stream = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    res = run_mixed([(runners[N], jobs[N]) for N in idx])
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    t = e0.elapsed_time(e1) / 1e3
+    out = {"workload": f"{n_mocks} lognormal mocks, n log-uniform [2e5, 2e6], half 256^3 / half 128^3, L=1500, "
+                       "CIC+interlacing, l=0,2 (device-generated catalogues)",
+           "mocks_per_s": n_mocks / t, "particles_per_s": float(counts.sum()) / t, "ms_total": t * 1e3,
+           "generation_s": t_gen, "lanes_per_mesh": 3}
+    for N, r in zip(idx, res):
+        mean, cov = covariance(r.pk.cpu().numpy(), ells_index=(0, 1))
+        out[f"covariance_{N}"] = {"mocks": int(len(idx[N])), "data_vector": int(mean.size),
+                                  "finite": bool(np.isfinite(cov).all())}
+    for r in runners.values():
+        r.close()
+    return out
+
+
+def serving_leg(dev, seed: int, seconds: float = 1.0, rate: float = 200.0) -> dict:
+    """Serving stream: Poisson arrivals (mean `rate`/s) for `seconds`; mesh 128/256/512 w.p. 0.5/0.35/0.15,
+    particle counts log-uniform [1e5, 1e7], MAS CIC or TSC, L from U[500, 2500]; 80 GB budget.
+    Client data: a pool of 8 device-generated lognormal catalogues of 1e7 particles (one box each, drawn from
+    U[500, 2500]) copied to pinned host memory; a request takes the first n particles of one of them."""
+    import torch
+    from gbpowspec.serve import Request, Server, percentiles
+    from gbpowspec.synth import lognormal_catalogue_gpu
+    rng = np.random.default_rng(seed)
+    pool = []
+    for i in range(8):
+        box = float(rng.uniform(500.0, 2500.0))
+        x, y, z = lognormal_catalogue_gpu(10_000_000, box, grid=256, seed=seed * 7919 + i, device=dev)
+        pool.append((box, [t.cpu().pin_memory() for t in (x, y, z)]))
+    torch.cuda.synchronize(dev)
+    n_req = max(1, int(rng.poisson(rate * seconds)))
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n_req))
+    reqs = []
+    for i in range(n_req):
+        box, (x, y, z) = pool[int(rng.integers(len(pool)))]
+        n = int(np.exp(rng.uniform(np.log(1e5), np.log(1e7))))
+        N = int(rng.choice([128, 256, 512], p=[0.5, 0.35, 0.15]))
+        mas = str(rng.choice(["cic", "tsc"]))
+        reqs.append(Request(x[:n], y[:n], z[:n], box=box, n_mesh=N, mas=mas))
+    srv = Server(budget_bytes=80e9, lanes_per_class=2, capacity=10_000_000, device=dev)
+    # warm every class once (lane creation and graph capture are not part of the stream)
+    for N in (128, 256, 512):
+        for mas in ("cic", "tsc"):
+            box, (x, y, z) = pool[0]
+            for _ in range(2):                                   # both lanes of the class
+                srv.submit(Request(x[:1000], y[:1000], z[:1000], box=box, n_mesh=N, mas=mas))
+    srv.drain(timeout=300)
+    results = []
+    t0 = time.perf_counter()
+    for a, r in zip(arrivals, reqs):
+        while time.perf_counter() - t0 < a:
+            results.extend(srv.poll())
+        srv.submit(r)
+    results.extend(srv.drain(timeout=300))
+    t_end = time.perf_counter() - t0
+    resident = srv.used
+    srv.close()
+    ok = [r for r in results if r.error is None]
+    lat = [r.latency for r in ok]
+    p = percentiles(lat)
+    return {"workload": f"Poisson arrivals {rate:g}/s for {seconds:g} s; mesh 128/256/512 (0.5/0.35/0.15); "
+                        "n log-uniform [1e5, 1e7]; CIC/TSC; L in [500, 2500]; 80 GB budget",
+            "requests": n_req, "completed": len(ok), "failed": len(results) - len(ok),
+            "p50_ms": None if p["p50"] is None else p["p50"] * 1e3,
+            "p99_ms": None if p["p99"] is None else p["p99"] * 1e3,
+            "throughput_rps": len(ok) / t_end, "particles_per_s": sum(r.n_kept for r in ok) / t_end,
+            "lanes_per_class": 2, "resident_lanes_gb": resident / 1e9}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -210,6 +309,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--n-mesh", type=int, default=None, help="override the mesh side (profiling cases)")
     ap.add_argument("--n-particles", type=int, default=None, help="override the particle count")
+    ap.add_argument("--no-covariance", action="store_true", help="skip the batched covariance leg")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving leg")
+    ap.add_argument("--serve-seconds", type=float, default=1.0)
     ap.add_argument("--profile-only", action="store_true",
                     help="plain path only, warm-up + timed steps (no other legs): a short command for ncu")
     args = ap.parse_args()
@@ -322,6 +424,12 @@ def main():
         dist.all_reduce(times, op=dist.ReduceOp.MAX)
     t_batch, t_e2e, t_plain = (float(v) for v in times)
 
+    extra = {}
+    if not args.no_covariance:
+        extra["batched_covariance"] = covariance_leg(dev, seed=3000 + rank)
+    if not args.no_serve:
+        extra["serving"] = serving_leg(dev, seed=4000 + rank, seconds=args.serve_seconds)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         t_cpu = cpu_reference_mock(x, y, z)
@@ -367,6 +475,7 @@ def main():
                 "path": "ParticleArena.upload (pinned H2D of every mock) + BatchRunner.run + P_l D2H"},
         "gpu_launches": int(round(per_mock_launches)) * args.steps * B + lanes * args.steps,
         "clocks": clk,
+        **extra,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -298,6 +298,23 @@ int gbp_particles_power_job(const gbp_job* job, int64_t capacity,
                             gbp_deposit_stats* stats_out, void* workspace,
                             size_t workspace_bytes, gbp_stream_t stream);
 
+/* ---- Lognormal mock catalogues on the device (no reference counterpart;
+ * the recipe of tests/create_lognormal.py:42-55, src/gauss_field.py:5-80,
+ * src/populate_field.py:11-29 with the benchmark's choices): Gaussian field
+ * on grid^3 with P_G(k) = A k exp(-(k/k_cut)^2), unit lattice variance,
+ * rho = exp(g - 1/2), exactly n particles drawn with probability
+ * proportional to rho, uniform in their cell, z shifted by N(0, sigma_v),
+ * periodic.  Philox4x32-10 counter-based random numbers: the catalogue is a
+ * pure function of the arguments.  grid even, 4..1024. */
+int gbp_lognormal_workspace_size(int grid, size_t* bytes);
+int gbp_lognormal(int grid, double box, double k_cut, double sigma_v,
+                  int64_t n, unsigned long long seed, float* x, float* y,
+                  float* z, void* workspace, size_t workspace_bytes,
+                  gbp_stream_t stream);
+/* Host evaluation of the generator's Philox4x32-10 block (known-answer
+ * tests): out = philox(ctr[4], key[2]). */
+int gbp_philox4x32_10(const unsigned* ctr, const unsigned* key, unsigned* out);
+
 /* ---- Lanes: resident per-mock pipelines for batching and serving --------
  * No reference counterpart (the reference computes one mock per call).
  * A lane owns every buffer one mock needs and, with GBP_LANE_GRAPH, a CUDA

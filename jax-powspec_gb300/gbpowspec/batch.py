@@ -84,15 +84,37 @@ class ParticleArena:
                 hv[3, a:b] = 1.0 if len(c) < 4 or c[3] is None else np.asarray(c[3], np.float32).reshape(-1)
         self.dev = torch.empty_like(self.host, device=self.device)
 
+    @classmethod
+    def empty(cls, counts, device=None, weighted: bool = False) -> "ParticleArena":
+        """A device-only arena for mocks of the given sizes (filled on the device, e.g. by the
+        lognormal generator through views(i)); upload() is not available."""
+        self = cls.__new__(cls)
+        self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
+        self.weighted = bool(weighted)
+        self.counts = np.asarray(counts, dtype=np.int64)
+        self.offsets = np.zeros(len(self.counts) + 1, dtype=np.int64)
+        np.cumsum(self.counts, out=self.offsets[1:])
+        self.host = None
+        self.dev = torch.empty((4 if weighted else 3, max(int(self.offsets[-1]), 1)), dtype=torch.float32,
+                               device=self.device)
+        return self
+
+    def views(self, i: int) -> tuple:
+        """Device views (x, y, z[, w]) of mock i."""
+        a, b = int(self.offsets[i]), int(self.offsets[i + 1])
+        return tuple(self.dev[k, a:b] for k in range(self.dev.shape[0]))
+
     def __len__(self) -> int:
         return len(self.counts)
 
     @property
     def nbytes(self) -> int:
-        return self.host.numel() * 4
+        return self.dev.numel() * 4
 
     def upload(self) -> int:
         """Enqueue the host-to-device copy of every mock; returns the bytes copied."""
+        if self.host is None:
+            raise RuntimeError("this arena lives on the device only")
         self.dev.copy_(self.host, non_blocking=True)
         return self.nbytes
 

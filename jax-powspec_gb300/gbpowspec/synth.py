@@ -17,7 +17,7 @@ from __future__ import annotations
 
 import numpy as np
 
-__all__ = ["uniform_catalogue", "lognormal_catalogue", "lognormal_density"]
+__all__ = ["uniform_catalogue", "lognormal_catalogue", "lognormal_density", "lognormal_catalogue_gpu"]
 
 
 def _clamp_box(a: np.ndarray, box: float) -> np.ndarray:
@@ -75,3 +75,32 @@ def lognormal_catalogue(n: int, box: float, grid: int = 256, seed: int = 0, rsd_
         z = z + rng.normal(0.0, rsd_sigma, size=n)
     perm = rng.permutation(n)
     return _clamp_box(x[perm], box), _clamp_box(y[perm], box), _clamp_box(z[perm], box)
+
+
+def lognormal_catalogue_gpu(n: int, box: float, grid: int = 256, seed: int = 0, rsd_sigma: float = 3.0,
+                            k_cut: float = 0.3, device=None, out=None):
+    """The same recipe generated on the device (gbp_lognormal): (x, y, z) float32 CUDA tensors.
+
+    The random numbers differ from the host generator's (counter-based
+    Philox4x32-10 instead of numpy's), so catalogues agree in distribution,
+    not value by value.  `out` = (x, y, z) tensors of >= n elements to reuse.
+    """
+    import ctypes as C
+
+    import torch
+
+    from . import _lib, _native
+    dev = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
+    lib = _lib.load()
+    need = C.c_size_t(0)
+    _lib.check(lib.gbp_lognormal_workspace_size(int(grid), C.byref(need)), "gbp_lognormal_workspace_size")
+    ws = _native.workspace(need.value, dev)
+    if out is None:
+        out = tuple(torch.empty(int(n), dtype=torch.float32, device=dev) for _ in range(3))
+    x, y, z = out
+    _lib.check(lib.gbp_lognormal(int(grid), float(box), float(k_cut), float(rsd_sigma), int(n),
+                                 int(seed) & 0xFFFFFFFFFFFFFFFF, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()),
+                                 C.c_void_p(z.data_ptr()), C.c_void_p(ws.data_ptr()), ws.numel(),
+                                 _native._stream_of(dev)), "gbp_lognormal")
+    return x[:n], y[:n], z[:n]
+
