@@ -418,11 +418,9 @@ def main():
         e2e_step()
     t_e2e = timed(e2e_step, args.steps)
 
-    # max over ranks
-    times = torch.tensor([t_batch, t_e2e, t_plain], dtype=torch.float64, device=dev)
-    if ws > 1:
-        dist.all_reduce(times, op=dist.ReduceOp.MAX)
-    t_batch, t_e2e, t_plain = (float(v) for v in times)
+    # the whole job ends when the slowest rank does
+    from gbpowspec.replicas import max_over_ranks
+    t_batch, t_e2e, t_plain = max_over_ranks([t_batch, t_e2e, t_plain])
 
     extra = {}
     if not args.no_covariance:
