@@ -35,8 +35,9 @@ def _errors(res_pk, ref):
     return [float(np.max(np.abs(res_pk[full, l] - ref["pk"][full, l]) / amp)) for l in range(3)]
 
 
+@pytest.mark.parametrize("interlace", [False, True])
 @pytest.mark.parametrize("N,n", [(256, 2_000_000), (1024, 16_777_216)])
-def test_precision_cic_pcs_against_fp64(N, n):
+def test_precision_cic_pcs_against_fp64(N, n, interlace):
     _need(40 if N == 1024 else 4)
     import fp64_torch as F
     from gbpowspec import PkConfig, PowerSpectrum
@@ -45,14 +46,15 @@ def test_precision_cic_pcs_against_fp64(N, n):
     x, y, z = _catalogue(n, box)
     report = {}
     for mas, order in (("cic", 2), ("pcs", 4)):
-        cfg = PkConfig(n_mesh=N, box_size=box, mas=mas, interlace=True, k_edges_kf=tuple(shell_edges(N).tolist()))
+        cfg = PkConfig(n_mesh=N, box_size=box, mas=mas, interlace=interlace,
+                       k_edges_kf=tuple(shell_edges(N).tolist()))
         ps = PowerSpectrum(cfg)
         res = ps.run(x, y, z)
         pk = res.pk.cpu().numpy()
         nm = res.nmodes.cpu().numpy()
         del ps
         torch.cuda.empty_cache()
-        ref = F.power_multipoles(x, y, z, box=box, N=N, mas=order, interlace=True, kedges_grid=shell_edges(N))
+        ref = F.power_multipoles(x, y, z, box=box, N=N, mas=order, interlace=interlace, kedges_grid=shell_edges(N))
         torch.cuda.empty_cache()
         np.testing.assert_array_equal(nm, ref["nmodes"])
         err = _errors(pk, ref)
@@ -61,8 +63,8 @@ def test_precision_cic_pcs_against_fp64(N, n):
         assert max(err) <= 1e-5, (mas, err)
     path = os.environ.get("GBP_PRECISION_REPORT")
     if path:
-        with open(f"{path}.{N}.json", "w") as f:
-            json.dump({"mesh": N, "particles": n, "box": box, **report}, f, indent=1)
+        with open(f"{path}.{N}.{'interlaced' if interlace else 'single'}.json", "w") as f:
+            json.dump({"mesh": N, "particles": n, "box": box, "interlace": interlace, **report}, f, indent=1)
 
 
 @pytest.mark.parametrize("N,n", [(256, 2_000_000), (1024, 16_777_216)])
