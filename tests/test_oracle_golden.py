@@ -85,3 +85,23 @@ def test_truth_deposit_conserves_mass(mas):
     w = rng.uniform(0.1, 3, 500).astype(np.float32)
     m = T.deposit(x, y, z, w, 10, np.float32(10 / 50), mas=mas, interlace=True)
     np.testing.assert_allclose(m.sum(axis=(1, 2, 3)), w.astype(np.float64).sum(), rtol=1e-12)
+
+
+def test_fast_cpu_stand_in_agrees_with_the_restatement():
+    """oracle/reference_fast (the timed CPU stand-in) vs oracle/reference_f32 on one small mock."""
+    from oracle import reference_f32 as R
+    from oracle import reference_fast as F
+    from gbpowspec.synth import lognormal_catalogue
+    N, box = 32, 500.0
+    x, y, z = lognormal_catalogue(30_000, box, grid=32, seed=3)
+    kf = 2 * np.pi / box
+    edges = np.arange(kf, np.pi * N / box, kf).astype(np.float32)
+    d = R.cic_mas_vec(np.zeros((N, N, N), np.float32), x, y, z, None, x.size, 0.0, 0.0, 0.0, box, N, True)
+    d = d / d.mean() - np.float32(1.0)
+    k0, p0, n0 = R.powspec_vec(d, box, edges)
+    k1, p1, n1 = F.reference_mock(x, y, z, box, N, edges)
+    np.testing.assert_array_equal(n0, n1)
+    np.testing.assert_allclose(k0, k1, rtol=0)
+    np.testing.assert_allclose(p1[:, 0], p0[:, 0], rtol=1e-4)
+    amp = np.abs(p0[:, 0])[:, None]
+    assert np.all(np.abs(p1[:, 1:] - p0[:, 1:]) <= 1e-4 * amp)
