@@ -37,13 +37,13 @@ struct ColTile {
   static constexpr int TY = 4;
   static constexpr int NPEN = TX * TY;            // pencils per tile; pencil f = lx * TY + ly
   static constexpr int PAIRS = NPEN / 2;          // complex transforms (pencils 2q, 2q+1)
-  static constexpr int NFFT = PAIRS * N / 8;      // radix-8 butterflies per stage
+  static constexpr int NFFT = PAIRS * N / 16;     // butterfly pairs (two columns) per radix-8 stage
   static constexpr int NT = NFFT < 256 ? 256 : NFFT;
   static constexpr size_t SMEM = (size_t)NPEN * N * 2 * sizeof(unsigned);   // low + high words
 };
 
 template <int N, int MAS, int G>
-__global__ void __launch_bounds__(ColTile<N>::NT, ColTile<N>::NT >= 512 ? 3 : 2)
+__global__ void __launch_bounds__(ColTile<N>::NT, 3)
 deposit_fftz_kernel(DepGeom g, const float4* __restrict__ entries, const unsigned* __restrict__ counts,
                     const unsigned* __restrict__ cursors, const DepCounters* ctr, const float2* __restrict__ tw,
                     float2* __restrict__ spec, long long* __restrict__ tile_mass) {
@@ -53,7 +53,7 @@ deposit_fftz_kernel(DepGeom g, const float4* __restrict__ entries, const unsigne
   extern __shared__ __align__(16) unsigned acc32[];
   unsigned* lo = acc32;                                // [NPEN][N] low words
   unsigned* hi = acc32 + NPEN * N;                     // [NPEN][N] high words
-  float2* cs = reinterpret_cast<float2*>(acc32);       // [PAIRS][N] complex, aliases the low words
+  float4* cs4 = reinterpret_cast<float4*>(acc32);      // [PAIRS/2][N] slots of two columns, alias the low words
   __shared__ long long s_part[NT / 32];
   const int tid = threadIdx.x;
   const int t = blockIdx.x;
@@ -114,27 +114,33 @@ deposit_fftz_kernel(DepGeom g, const float4* __restrict__ entries, const unsigne
     }
     __syncthreads();
 
-    // z transform: pencils 2q and 2q+1 are the real and imaginary parts of column q
+    // z transform: pencils 2q and 2q+1 are the real and imaginary parts of
+    // column q; a thread transforms columns 2cp and 2cp+1 (pencils 4cp..4cp+3)
     long long part = 0;
-    auto gin = [&part, inv_sc, lo, hi](int j, int q) {
-      const int c0 = (2 * q) * N + j, c1 = c0 + N;
-      const long long a = (long long)(((unsigned long long)hi[c0] << 32) | lo[c0]);
-      const long long b = (long long)(((unsigned long long)hi[c1] << 32) | lo[c1]);
-      part += a + b;
-      return make_float2(fixed_to_float(a, inv_sc), fixed_to_float(b, inv_sc));
+    auto gin = [&part, inv_sc, lo, hi](int j, int cp) {
+      float v[4];
+#pragma unroll
+      for (int f = 0; f < 4; ++f) {
+        const int c = (4 * cp + f) * N + j;
+        const long long a = (long long)(((unsigned long long)hi[c] << 32) | lo[c]);
+        part += a;
+        v[f] = fixed_to_float(a, inv_sc);
+      }
+      return make_float4(v[0], v[1], v[2], v[3]);
     };
-    auto sin_ = [cs](int j, int q) { return cs[q * N + fft::zsw(j)]; };
-    auto sout = [cs](int j, int q, float2 v) { cs[q * N + fft::zsw(j)] = v; };
-    fft::run_stages<N, PAIRS, NT, true, true, true>(gin, sin_, sout, sout, tw, tid);
+    auto sin_ = [cs4](int j, int cp) { return cs4[cp * N + fft::zsw(j)]; };
+    auto sout = [cs4](int j, int cp, float4 v) { cs4[cp * N + fft::zsw(j)] = v; };
+    fft::run_stages2<N, PAIRS / 2, NT, true, true, true>(gin, sin_, sout, sout, tw, tid);
 
     // split the packed spectra; write all pencils' rows (row padding -> 0)
+    const float2* cs = reinterpret_cast<const float2*>(cs4);
     float2* out = spec + grid * gstride;
     for (int idx = tid; idx < PAIRS * P; idx += NT) {
       const int q = idx / P, k = idx - (idx / P) * P;
       float2 a = make_float2(0.f, 0.f), b = make_float2(0.f, 0.f);
       if (k <= H) {
-        const float2 c = cs[q * N + fft::zsw(k)];
-        const float2 m = cs[q * N + fft::zsw((N - k) & (N - 1))];
+        const float2 c = cs[((q >> 1) * N + fft::zsw(k)) * 2 + (q & 1)];
+        const float2 m = cs[((q >> 1) * N + fft::zsw((N - k) & (N - 1))) * 2 + (q & 1)];
         const float2 cm = make_float2(m.x, -m.y);
         const float2 sum = fft::cadd(c, cm), dif = fft::cmi(fft::csub(c, cm));
         a = make_float2(0.5f * sum.x, 0.5f * sum.y);

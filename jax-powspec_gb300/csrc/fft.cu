@@ -35,46 +35,48 @@ using fft::csub;
 __host__ __device__ constexpr int zpitch(int N) { return N / 2 + 8; }
 
 // ---- z pass ---------------------------------------------------------------
-// PAIRS complex columns (2*PAIRS real pencils) per CTA, NT = PAIRS * N / 8.
-// Consecutive lanes take consecutive z, so the first stage's loads of each
-// pencil are 128-byte coalesced.  Shared memory is column-major, column q
-// holding pair q, with row j stored at fft::zsw(j) (conflict-free for every
-// stage).  The last stage stays in shared memory, where each half spectrum
-// needs C[k] and C[N-k] together.
+// PAIRS complex columns (2*PAIRS real pencils) per CTA; a thread transforms
+// two columns (four pencils) at once, NT = (PAIRS / 2) * N / 8.  Consecutive
+// lanes take consecutive z, so the first stage's loads of each pencil are
+// 128-byte coalesced.  Shared memory is column-major in 16-byte slots of two
+// columns (fft_pass.cuh).  The last stage stays in shared memory, where each
+// half spectrum needs C[k] and C[N-k] together.
 using fft::zsw;
 
 template <int N, int PAIRS>
-__global__ void __launch_bounds__(PAIRS * N / 8)
+__global__ void __launch_bounds__(PAIRS * N / 16)
 fftz_kernel(const float* __restrict__ mesh, float2* __restrict__ out, long long npencils,
             const float2* __restrict__ tw) {
-  constexpr int NT = PAIRS * N / 8;
+  constexpr int NT = PAIRS * N / 16;
+  constexpr int CP = PAIRS / 2;
   constexpr int P = zpitch(N);
   constexpr int H = N / 2;
-  constexpr int LD = N;
-  extern __shared__ __align__(16) float2 s[];     // [PAIRS][LD]
+  extern __shared__ __align__(16) float4 s4[];    // [CP][N] slots of two columns
   const int tid = threadIdx.x;
   const long long pen0 = (long long)blockIdx.x * 2 * PAIRS;
   const long long left = npencils - pen0;
   const int npen = left < 2 * PAIRS ? (int)left : 2 * PAIRS;
   const float* base = mesh + pen0 * N;
 
-  auto gin = [base, npen](int j, int q) {
-    const float a = 2 * q < npen ? __ldcs(base + (2 * q) * N + j) : 0.0f;
-    const float b = 2 * q + 1 < npen ? __ldcs(base + (2 * q + 1) * N + j) : 0.0f;
-    return make_float2(a, b);
+  auto gin = [base, npen](int j, int cp) {      // pencils 4cp .. 4cp+3 at z = j
+    float v[4];
+#pragma unroll
+    for (int f = 0; f < 4; ++f) v[f] = 4 * cp + f < npen ? __ldcs(base + (4 * cp + f) * N + j) : 0.0f;
+    return make_float4(v[0], v[1], v[2], v[3]);
   };
-  auto sin_ = [](int j, int q) { return s[q * LD + zsw(j)]; };
-  auto sout = [](int j, int q, float2 v) { s[q * LD + zsw(j)] = v; };
-  fft::run_stages<N, PAIRS, NT, true, true>(gin, sin_, sout, sout, tw, tid);
+  auto sin_ = [](int j, int cp) { return s4[cp * N + zsw(j)]; };
+  auto sout = [](int j, int cp, float4 v) { s4[cp * N + zsw(j)] = v; };
+  fft::run_stages2<N, CP, NT, true, false, true>(gin, sin_, sout, sout, tw, tid);
 
   // split the packed spectra and write both pencils' rows (padding -> 0)
+  const float2* s2 = reinterpret_cast<const float2*>(s4);
   for (int idx = tid; idx < PAIRS * P; idx += NT) {
     const int q = idx / P, k = idx - (idx / P) * P;
     if (2 * q >= npen) continue;
     float2 a = make_float2(0.f, 0.f), b = make_float2(0.f, 0.f);
     if (k <= H) {
-      const float2 c = s[q * LD + zsw(k)];
-      const float2 m = s[q * LD + zsw((N - k) & (N - 1))];
+      const float2 c = s2[((q >> 1) * N + zsw(k)) * 2 + (q & 1)];
+      const float2 m = s2[((q >> 1) * N + zsw((N - k) & (N - 1))) * 2 + (q & 1)];
       const float2 cm = make_float2(m.x, -m.y);
       const float2 sum = cadd(c, cm), dif = cmi(csub(c, cm));
       a = make_float2(0.5f * sum.x, 0.5f * sum.y);
@@ -87,20 +89,24 @@ fftz_kernel(const float* __restrict__ mesh, float2* __restrict__ out, long long 
 
 // ---- y and x passes --------------------------------------------------------
 // 8 adjacent kz columns x N rows per CTA, rows `row_stride` complex apart;
-// CTA b covers plane (b / nkb) and kz block (b % nkb).  N threads: one
-// radix-8 butterfly each per stage; the first stage loads from HBM and the
-// last stores to HBM (fft_pass.cuh), in place.
+// CTA b covers plane (b / nkb) and kz block (b % nkb).  N/2 threads: one
+// pair of radix-8 butterflies (two columns) each per stage; the first stage
+// loads from HBM and the last stores to HBM (fft_pass.cuh), in place.
 template <int N>
-__global__ void __launch_bounds__(N, 2048 / N < 3 ? 2048 / N : 3)
+__global__ void __launch_bounds__(N / 2, N <= 512 ? 4 : 2)
 fft_cols_kernel(float2* __restrict__ data, long long plane_stride, long long row_stride, int nplanes, int nkb,
                 const float2* __restrict__ tw) {
   extern __shared__ __align__(16) float2 s[];
   const int plane = blockIdx.x / nkb, kb = blockIdx.x % nkb;
   if (plane >= nplanes) return;
   float2* base = data + plane * plane_stride + kb * 8;
-  auto gin = [base, row_stride](int j, int col) { return __ldcs(base + j * row_stride + col); };
-  auto gout = [base, row_stride](int j, int col, float2 v) { __stcs(base + j * row_stride + col, v); };
-  fft::col_fft<N, 1, N, false>(s, gin, gout, tw, threadIdx.x);
+  auto gin = [base, row_stride](int j, int cp) {
+    return __ldcs(reinterpret_cast<const float4*>(base + j * row_stride) + cp);
+  };
+  auto gout = [base, row_stride](int j, int cp, float4 v) {
+    __stcs(reinterpret_cast<float4*>(base + j * row_stride) + cp, v);
+  };
+  fft::col_fft<N, 1, N / 2, false>(s, gin, gout, tw, threadIdx.x);
 }
 
 template <int N>
@@ -118,7 +124,7 @@ int run_fft(const float* mesh, float2* spec, int G, const float2* tw, cudaStream
     GBP_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const long long blocks = (npen + 2 * PAIRS - 1) / (2 * PAIRS);
     GBP_TRACE("fft_z", st);
-    k<<<(unsigned)blocks, PAIRS * N / 8, smem, st>>>(mesh, spec, npen, tw);
+    k<<<(unsigned)blocks, PAIRS * N / 16, smem, st>>>(mesh, spec, npen, tw);
     GBP_LAUNCH_CHECK();
   }
   const int nkb = P / C;
@@ -127,13 +133,14 @@ int run_fft(const float* mesh, float2* spec, int G, const float2* tw, cudaStream
   GBP_CUDA_TRY(cudaFuncSetAttribute(kc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   {  // y pass: a plane is one x slab of one grid; rows (y) are P apart
     GBP_TRACE("fft_y", st);
-    kc<<<(unsigned)(G * N * nkb), N, smem, st>>>(spec, (long long)N * P, P, G * N, nkb, tw);
+    kc<<<(unsigned)(G * N * nkb), N / 2, smem, st>>>(spec, (long long)N * P, P, G * N, nkb, tw);
     GBP_LAUNCH_CHECK();
   }
   // x pass: a plane is one y row of one grid; rows (x) are N*P apart
   for (int g = 0; x_pass && g < G; ++g) {
     GBP_TRACE("fft_x", st);
-    kc<<<(unsigned)(N * nkb), N, smem, st>>>(spec + (long long)g * N * N * P, P, (long long)N * P, N, nkb, tw);
+    kc<<<(unsigned)(N * nkb), N / 2, smem, st>>>(spec + (long long)g * N * N * P, P, (long long)N * P, N, nkb,
+                                                 tw);
     GBP_LAUNCH_CHECK();
   }
   return GBP_OK;
@@ -145,15 +152,45 @@ int run_fft(const float* mesh, float2* spec, int G, const float2* tw, cudaStream
 bool own_fft_supported(int N) { return N == 64 || N == 128 || N == 256 || N == 512 || N == 1024; }
 int own_fft_pitch(int N) { return zpitch(N); }
 
-int own_fft_twiddles(int N, float2** d_tw) {
-  std::vector<float2> h((size_t)N);
+// Twiddles of an N-point transform: exp(-2 pi i e / N) for e < N, then one
+// table per stage of span p > 1 (radix R): entry k * 8 + r holds
+// exp(-2 pi i r k / (R p)) for r < R (fft_pass.cuh reads them as float4s).
+template <int N>
+std::vector<float2> twiddle_tables() {
+  std::vector<float2> h((size_t)fft::tw_size<N>(), make_float2(0.f, 0.f));
   for (int e = 0; e < N; ++e) {
     const double a = -2.0 * M_PI * (double)e / (double)N;
     h[e] = make_float2((float)cos(a), (float)sin(a));
   }
+  using RD = fft::Radices<N>;
+  int p = 1;
+  for (int st = 0; st < RD::stages; ++st) {
+    const int R = st < RD::n8 ? 8 : (RD::tail == 1 ? 2 : 4);
+    if (p > 1) {
+      for (int k = 0; k < p; ++k)
+        for (int r = 0; r < R; ++r) {
+          const double a = -2.0 * M_PI * (double)r * (double)k / ((double)R * (double)p);
+          h[(size_t)fft::tw_off<N>(p) + (size_t)k * 8 + r] = make_float2((float)cos(a), (float)sin(a));
+        }
+    }
+    p *= R;
+  }
+  return h;
+}
+
+int own_fft_twiddles(int N, float2** d_tw) {
+  std::vector<float2> h;
+  switch (N) {
+    case 64: h = twiddle_tables<64>(); break;
+    case 128: h = twiddle_tables<128>(); break;
+    case 256: h = twiddle_tables<256>(); break;
+    case 512: h = twiddle_tables<512>(); break;
+    case 1024: h = twiddle_tables<1024>(); break;
+    default: return GBP_ERR_UNSUPPORTED;
+  }
   float2* d = nullptr;
-  if (cudaMalloc(&d, (size_t)N * sizeof(float2)) != cudaSuccess) return GBP_ERR_ALLOC;
-  const cudaError_t ce = cudaMemcpy(d, h.data(), (size_t)N * sizeof(float2), cudaMemcpyHostToDevice);
+  if (cudaMalloc(&d, h.size() * sizeof(float2)) != cudaSuccess) return GBP_ERR_ALLOC;
+  const cudaError_t ce = cudaMemcpy(d, h.data(), h.size() * sizeof(float2), cudaMemcpyHostToDevice);
   if (ce != cudaSuccess) {
     set_last_cuda_error(ce);
     cudaFree(d);

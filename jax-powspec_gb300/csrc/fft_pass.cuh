@@ -1,23 +1,29 @@
-// Column-FFT engine for the y and x passes: C columns x N rows per CTA,
-// radix-8 Stockham stages (fft_core.cuh) whose first stage reads its inputs
-// straight from global memory and whose last stage writes its outputs
-// straight to their destination (global memory, or a transposed shared
-// buffer).  Only the exchanges between stages go through shared memory, so
-// each element costs 4 shared-memory accesses per pass instead of 8 (a
-// staged load, three in-place stages and a staged store).
+// Column-FFT engine shared by every pass of the library transform: radix-8
+// Stockham stages (fft_core.cuh) over blocks of columns, where
 //
-// Shared layout of a block of 8 columns: row j holds the 8 complex values of
-// the columns (64 bytes).  Row j is stored at physical row j ^ bit3(j): a
-// warp touches 4 aligned rows per access, which then fall on alternating
-// halves of the 128-byte bank line (the minimum of 2 wavefronts for 32 x 8
-// bytes) both in the stride-8 writes of the first stage and in the
-// consecutive-row accesses of the others.  Two slabs of 8 columns (two
-// grids) are offset by 64 bytes, so a half-warp's 16 columns of one row
-// cover one whole bank line.
+//   * each thread transforms the same butterfly of two adjacent columns at
+//     once: every shared or global access moves 16 bytes (two complex
+//     values), and the two butterflies share one set of twiddle factors;
+//   * the twiddles come from per-stage tables, w_r(k) = exp(-2 pi i r k /
+//     (R p)) for r < 8 stored contiguously per k (four 16-byte loads);
+//   * the first stage reads its inputs from wherever they are (HBM, or
+//     integer accumulators) and the last stage writes its outputs to
+//     wherever they go (HBM, or a transposed shared buffer); only the
+//     exchanges between stages go through shared memory.
 //
-// Thread b of a stage owns butterfly (col = b % COLS, i = b / COLS).  The
-// forward transform is exp(-2 pi i j k / N) (cuFFT, numpy), natural-order
-// output.
+// Two shared layouts, both free of bank conflicts for every stage's access
+// pattern (checked by enumeration):
+//
+//   ColBlock (thread b owns column pair b % CP, butterfly b / CP): row j of a
+//     block of 8 columns is 64 bytes, stored at physical row j ^ bit3(j), so
+//     the two rows of a quarter-warp fall on the two halves of a 128-byte
+//     bank line; two slabs (two grids) are offset by 64 bytes.
+//   Column-major pairs (IFAST: consecutive lanes on consecutive rows): the
+//     16-byte slot of rows j of two adjacent columns is at j ^ ((j >> 3) & 7),
+//     so 8 consecutive rows of any stage (the stride-8 writes of the first
+//     stage included) hit 8 distinct slots.
+//
+// Forward transform exp(-2 pi i j k / N) (cuFFT, numpy), natural-order output.
 #pragma once
 
 #include "fft_core.cuh"
@@ -25,58 +31,83 @@
 namespace gbp {
 namespace fft {
 
-// Row position of element j in a column-major block walked with consecutive
-// lanes on consecutive rows (IFAST stages): bits 4-6 of j are XORed into bits
-// 0-3, which puts the 16 lanes of a half-warp on 16 distinct 8-byte bank slots
-// in every stage (the stride-8 writes of the first stage, the two
-// interleaved runs of the second, the consecutive rows of the others).
-__device__ __forceinline__ int zsw(int j) { return j ^ ((j >> 4) & 7) ^ (((j >> 6) & 1) << 3); }
+// Offset (in float2) of the twiddle table of the stage with span p > 1; the
+// first N entries of the table buffer are exp(-2 pi i e / N).
+template <int N>
+__host__ __device__ constexpr int tw_off(int p) { return N + 8 * (p - 8) / 7; }
 
-template <int N, int SLABS>
-struct ColBlock {
-  static constexpr int COLS = 8 * SLABS;
-  static constexpr int SLAB = N * 8 + 8;    // complex per slab (+8: the 64-byte shift of slab 1)
-  __device__ static __forceinline__ int row(int j) { return SLABS == 1 ? (j ^ ((j >> 3) & 1)) : j; }
-  __device__ static __forceinline__ int at(int j, int col) { return (col >> 3) * SLAB + row(j) * 8 + (col & 7); }
-};
+// Size (in float2) of the whole twiddle buffer for N.
+template <int N>
+constexpr int tw_size() {
+  int p = 1;
+  for (int s = 0; s < Radices<N>::n8; ++s) p *= 8;   // span of the last radix-8 stage's successor
+  return tw_off<N>(p) + 8 * p;
+}
 
-// One stage.  In(row, col) -> float2 gives the inputs, Out(row, col, v)
-// takes the outputs; MID_SYNC separates the reads from the writes (in-place
-// shared stages), END_SYNC publishes the writes to the next stage.  Thread
-// b owns butterfly (col = b % COLS, i = b / COLS), or with IFAST (i = b %
-// (N/R), col = b / (N/R)): consecutive lanes on consecutive rows.
-template <int N, int R, int COLS, int NT, bool MID_SYNC, bool END_SYNC, bool IFAST = false, class In, class Out>
-__device__ __forceinline__ void stage_io(In in, Out out, const float2* __restrict__ tw, int p, int tid) {
-  constexpr int NB = COLS * (N / R);
+__device__ __forceinline__ float2 lo2(float4 v) { return make_float2(v.x, v.y); }
+__device__ __forceinline__ float2 hi2(float4 v) { return make_float2(v.z, v.w); }
+__device__ __forceinline__ float4 pack2(float2 a, float2 b) { return make_float4(a.x, a.y, b.x, b.y); }
+
+// One stage over CP column pairs.  In(row, cp) -> float4, Out(row, cp, float4).
+// MID_SYNC separates the reads from the writes (in-place shared stages);
+// END_SYNC publishes the writes.  IFAST: thread b owns butterfly b % (N/R) of
+// column pair b / (N/R) (consecutive lanes, consecutive rows); otherwise
+// column pair b % CP, butterfly b / CP.
+template <int N, int R, int CP, int NT, bool MID_SYNC, bool END_SYNC, bool IFAST, class In, class Out>
+__device__ __forceinline__ void stage2(In in, Out out, const float2* __restrict__ tw, int p, int tid) {
+  constexpr int NB = CP * (N / R);
   constexpr int PER = (NB + NT - 1) / NT;
-  float2 u[PER][R];
+  float4 u[PER][R];
 #pragma unroll
   for (int q = 0; q < PER; ++q) {
     const int b = tid + q * NT;
     if (PER * NT != NB && b >= NB) continue;
-    const int col = IFAST ? b / (N / R) : b % COLS, i = IFAST ? b % (N / R) : b / COLS;
-    const int k = i & (p - 1);
+    const int cp = IFAST ? b / (N / R) : b % CP, i = IFAST ? b % (N / R) : b / CP;
 #pragma unroll
-    for (int r = 0; r < R; ++r) u[q][r] = in(i + r * (N / R), col);
-    if (p > 1) {
-      const int step = N / (p * R);
+    for (int r = 0; r < R; ++r) u[q][r] = in(i + r * (N / R), cp);
+    float2 a[R], c[R];
 #pragma unroll
-      for (int r = 1; r < R; ++r) u[q][r] = cmul(u[q][r], __ldg(tw + ((r * k * step) & (N - 1))));
+    for (int r = 0; r < R; ++r) {
+      a[r] = lo2(u[q][r]);
+      c[r] = hi2(u[q][r]);
     }
-    if constexpr (R == 8) dft8(u[q]);
-    else if constexpr (R == 4) dft4(u[q]);
-    else dft2(u[q][0], u[q][1]);
+    if (p > 1) {
+      const int k = i & (p - 1);
+      const float4* t4 = reinterpret_cast<const float4*>(tw + tw_off<N>(p) + k * 8);
+#pragma unroll
+      for (int rr = 0; rr < R / 2; ++rr) {
+        const float4 w = __ldg(t4 + rr);
+        if (rr > 0) {
+          a[2 * rr] = cmul(a[2 * rr], lo2(w));
+          c[2 * rr] = cmul(c[2 * rr], lo2(w));
+        }
+        a[2 * rr + 1] = cmul(a[2 * rr + 1], hi2(w));
+        c[2 * rr + 1] = cmul(c[2 * rr + 1], hi2(w));
+      }
+    }
+    if constexpr (R == 8) {
+      dft8(a);
+      dft8(c);
+    } else if constexpr (R == 4) {
+      dft4(a);
+      dft4(c);
+    } else {
+      dft2(a[0], a[1]);
+      dft2(c[0], c[1]);
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r) u[q][r] = pack2(a[r], c[r]);
   }
   if (MID_SYNC) __syncthreads();
 #pragma unroll
   for (int q = 0; q < PER; ++q) {
     const int b = tid + q * NT;
     if (PER * NT != NB && b >= NB) continue;
-    const int col = IFAST ? b / (N / R) : b % COLS, i = IFAST ? b % (N / R) : b / COLS;
+    const int cp = IFAST ? b / (N / R) : b % CP, i = IFAST ? b % (N / R) : b / CP;
     const int k = i & (p - 1);
     const int j = (i - k) * R + k;
 #pragma unroll
-    for (int r = 0; r < R; ++r) out(j + r * p, col, u[q][r]);
+    for (int r = 0; r < R; ++r) out(j + r * p, cp, u[q][r]);
   }
   if (END_SYNC) __syncthreads();
 }
@@ -84,46 +115,58 @@ __device__ __forceinline__ void stage_io(In in, Out out, const float2* __restric
 // Full transform: the first stage reads `gin`, the stages in between go
 // through shared memory (`sin` / `sout`), the last stage writes `gout`.
 // Starts without a barrier (the caller orders earlier uses of shared
-// memory).  OUT_SHARED: `gout` writes the shared buffer the last stage
-// reads, so it reads everything first and ends with a barrier.  IN_SHARED:
-// `gin` reads shared memory that the first stage's writes alias, so the
-// first stage, too, reads everything before it writes.
-template <int N, int COLS, int NT, bool IFAST, bool OUT_SHARED, bool IN_SHARED = false, class GIn, class SIn,
-          class SOut, class GOut>
-__device__ __forceinline__ void run_stages(GIn gin, SIn sin_, SOut sout, GOut gout, const float2* __restrict__ tw,
-                                           int tid) {
+// memory).  IN_SHARED: `gin` reads shared memory that the first stage's
+// writes alias; OUT_SHARED: `gout` writes the shared memory the last stage
+// reads (each then reads everything before it writes; OUT_SHARED also ends
+// with a barrier).
+template <int N, int CP, int NT, bool IFAST, bool IN_SHARED, bool OUT_SHARED, class GIn, class SIn, class SOut,
+          class GOut>
+__device__ __forceinline__ void run_stages2(GIn gin, SIn sin_, SOut sout, GOut gout, const float2* __restrict__ tw,
+                                            int tid) {
   using RD = Radices<N>;
   static_assert(RD::stages >= 2, "at least two stages");
+  stage2<N, 8, CP, NT, IN_SHARED, true, IFAST>(gin, sout, tw, 1, tid);
+  int p = 8;
   if constexpr (RD::tail == 0) {
-    stage_io<N, 8, COLS, NT, IN_SHARED, true, IFAST>(gin, sout, tw, 1, tid);
-    int p = 8;
 #pragma unroll
     for (int st = 1; st < RD::n8 - 1; ++st) {
-      stage_io<N, 8, COLS, NT, true, true, IFAST>(sin_, sout, tw, p, tid);
+      stage2<N, 8, CP, NT, true, true, IFAST>(sin_, sout, tw, p, tid);
       p *= 8;
     }
-    stage_io<N, 8, COLS, NT, OUT_SHARED, OUT_SHARED, IFAST>(sin_, gout, tw, p, tid);
+    stage2<N, 8, CP, NT, OUT_SHARED, OUT_SHARED, IFAST>(sin_, gout, tw, p, tid);
   } else {
-    stage_io<N, 8, COLS, NT, IN_SHARED, true, IFAST>(gin, sout, tw, 1, tid);
-    int p = 8;
 #pragma unroll
     for (int st = 1; st < RD::n8; ++st) {
-      stage_io<N, 8, COLS, NT, true, true, IFAST>(sin_, sout, tw, p, tid);
+      stage2<N, 8, CP, NT, true, true, IFAST>(sin_, sout, tw, p, tid);
       p *= 8;
     }
-    if constexpr (RD::tail == 1) stage_io<N, 2, COLS, NT, OUT_SHARED, OUT_SHARED, IFAST>(sin_, gout, tw, p, tid);
-    else stage_io<N, 4, COLS, NT, OUT_SHARED, OUT_SHARED, IFAST>(sin_, gout, tw, p, tid);
+    if constexpr (RD::tail == 1) stage2<N, 2, CP, NT, OUT_SHARED, OUT_SHARED, IFAST>(sin_, gout, tw, p, tid);
+    else stage2<N, 4, CP, NT, OUT_SHARED, OUT_SHARED, IFAST>(sin_, gout, tw, p, tid);
   }
 }
 
-// Column blocks of 8 (x SLABS) columns in the ColBlock layout.
+// Blocks of 8 columns (x SLABS); a float4 holds two adjacent columns.
+template <int N, int SLABS>
+struct ColBlock {
+  static constexpr int COLS = 8 * SLABS;
+  static constexpr int CP = COLS / 2;
+  static constexpr int SLAB = N * 8 + 8;    // complex per slab (+8: the 64-byte shift of slab 1)
+  __device__ static __forceinline__ int row(int j) { return SLABS == 1 ? (j ^ ((j >> 3) & 1)) : j; }
+  // float4 index of column pair cp (columns 2cp, 2cp+1) in row j
+  __device__ static __forceinline__ int at(int j, int cp) { return (cp >> 2) * (SLAB / 2) + row(j) * 4 + (cp & 3); }
+};
+
 template <int N, int SLABS, int NT, bool OUT_SHARED, class In, class Out>
 __device__ __forceinline__ void col_fft(float2* s, In gin, Out gout, const float2* __restrict__ tw, int tid) {
   using L = ColBlock<N, SLABS>;
-  auto sin_ = [s](int j, int col) { return s[L::at(j, col)]; };
-  auto sout = [s](int j, int col, float2 v) { s[L::at(j, col)] = v; };
-  run_stages<N, L::COLS, NT, false, OUT_SHARED>(gin, sin_, sout, gout, tw, tid);
+  float4* s4 = reinterpret_cast<float4*>(s);
+  auto sin_ = [s4](int j, int cp) { return s4[L::at(j, cp)]; };
+  auto sout = [s4](int j, int cp, float4 v) { s4[L::at(j, cp)] = v; };
+  run_stages2<N, L::CP, NT, false, false, OUT_SHARED>(gin, sin_, sout, gout, tw, tid);
 }
+
+// Slot of row j in a column-major block of column pairs (IFAST stages).
+__device__ __forceinline__ int zsw(int j) { return j ^ ((j >> 3) & 7); }
 
 }  // namespace fft
 }  // namespace gbp

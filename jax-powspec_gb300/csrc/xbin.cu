@@ -220,10 +220,13 @@ xbin_kernel(PowGeom g) {
     for (int it = grp; it < g.items; it += g.groups) {
       const int y = it / g.nkb, kb = it - (it / g.nkb) * g.nkb;
       const float2* src = g.s0 + ((long long)y * P + kb * XB_C);
-      auto gin = [src, gstride](int x, int col) {
-        return __ldcs(src + (col >> 3) * gstride + (long long)x * N * P + (col & 7));
+      auto gin = [src, gstride](int x, int cp) {   // columns 2cp, 2cp+1 (slab = grid cp / 4)
+        return __ldcs(reinterpret_cast<const float4*>(src + (cp >> 2) * gstride + (long long)x * N * P) + (cp & 3));
       };
-      auto tout = [s](int x, int col, float2 v) { s[col * TST + xswz<N>(x)] = v; };
+      auto tout = [s](int x, int cp, float4 v) {
+        s[(2 * cp) * TST + xswz<N>(x)] = fft::lo2(v);
+        s[(2 * cp + 1) * TST + xswz<N>(x)] = fft::hi2(v);
+      };
       fft::col_fft<N, G, XB_THREADS, true>(s, gin, tout, g.tw, tid);   // ends with a barrier
       xbin_item<N, NV, INTER>(g, t, c2x, ephx, s, warp, lane, y, kb);  // ends with a barrier
     }
