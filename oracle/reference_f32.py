@@ -215,3 +215,60 @@ def powspec_vec_fundamental(delta, box_size):
         out[:, 1] = pk[:, 1] / nmodes * F32(5.0) * norm                       # :113
         out[:, 2] = pk[:, 2] / nmodes * F32(9.0) * norm                       # :114
     return k3d.astype(F32), out, nmodes
+
+
+def _xi_core(delta, box_size, s_edges, mu_zero_at_origin: bool):
+    """src/correlations.py:120-187 (xi_vec) and :692-712 (the xi half of compute_2pt_correlations)."""
+    dims = delta.shape[0]
+    box = _f32(box_size)
+    kF = F32(F32(2.0 * np.pi) / box)                                          # :124 / :646
+    s_edges = np.asarray(s_edges, F32)
+    k_edges = (((kF * s_edges).astype(F32) * F32(dims)).astype(F32) / box).astype(F32)   # :125 / :698
+    kedges = (k_edges / kF).astype(F32)                                       # :172 / :699
+    delta_k = scipy.fft.rfftn(np.asarray(delta, F32), axes=(0, 1, 2)).astype(np.complex64)
+    kx, ky, kz = _kgrid(dims)
+    corr = _cic_correction(kx, dims) * _cic_correction(ky, dims) * _cic_correction(kz, dims)
+    delta_k = (delta_k * corr).astype(np.complex64)                            # :147-148 / :666
+    delta2 = (delta_k * delta_k.conj()).astype(np.complex64)                   # :149 (complex)
+    if mu_zero_at_origin:
+        delta2 = delta2.real.astype(F32)                                       # :674 takes .real first
+    delta_xi = scipy.fft.irfftn(delta2.astype(np.complex64), s=delta.shape, axes=(0, 1, 2)).astype(F32)  # :151 / :697
+    middle = dims // 2
+    r = np.arange(dims, dtype=np.int32)
+    ki = np.where(r > middle, r - dims, r).astype(np.int32)
+    gx = ki[:, None, None]
+    gy = ki[None, :, None]
+    gz = ki[None, None, :]
+    kk = np.sqrt((gx * gx + gy * gy + gz * gz).astype(F32))                   # :158 / :692
+    with np.errstate(invalid="ignore", divide="ignore"):
+        mu = (np.broadcast_to(gz, kk.shape).astype(F32) / kk).astype(F32)      # :162 (0/0 -> NaN)
+        if mu_zero_at_origin:
+            mu = np.where(kk == 0, F32(0), mu).astype(F32)                    # :694
+    mu2 = (mu ** 2).ravel()
+    kf = kk.ravel()
+    w = delta_xi.ravel()
+    mono = histogram_f32(kf, kedges, w)
+    quad = histogram_f32(kf, kedges, w * (F32(3.0) * mu2 - F32(1.0)) / F32(2.0))
+    hexa = histogram_f32(kf, kedges, w * (F32(35.0) * mu2 * mu2 - F32(30.0) * mu2 + F32(3.0)) / F32(8.0))
+    nmodes = histogram_f32(kf, kedges, None)
+    nmodes = np.where(nmodes == 0, F32(np.inf), nmodes).astype(F32)          # :180 / :705
+    d3 = F32(dims ** 3)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        xi = np.zeros((mono.size, 3), F32)
+        xi[:, 0] = mono / nmodes / d3
+        xi[:, 1] = quad / nmodes * F32(5.0) / d3
+        xi[:, 2] = hexa / nmodes * F32(9.0) / d3
+    r3d = (F32(0.5) * (kedges[1:] + kedges[:-1])) * (box * F32(1.0) / F32(dims))   # :185 / :710
+    return r3d.astype(F32), xi, nmodes
+
+
+def xi_vec(delta, box_size, s_edges):
+    """src/correlations.py:120-187: (r3D, xi3D, Nmodes3D), mu = 0/0 = NaN at r = 0."""
+    return _xi_core(delta, box_size, s_edges, mu_zero_at_origin=False)
+
+
+def compute_2pt_correlations(delta, box_size, s_edges, k_edges):
+    """src/correlations.py:641-712: (k3D, Pk3D, Nmodes3D_pk, r3D, xi3D), mu = 0 at the origin."""
+    k3d, pk, nm = powspec_vec(delta, box_size, k_edges)
+    r3d, xi, _ = _xi_core(delta, box_size, s_edges, mu_zero_at_origin=True)
+    return k3d, pk, nm, r3d, xi

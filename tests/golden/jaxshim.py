@@ -16,7 +16,8 @@ Semantics restated from JAX's published behaviour with 64-bit mode off:
     equal to the last edge go to the last bin, then
     ``zeros(len(bins), weights.dtype).at[idx].add(weights)[1:]``;
   * ``jnp.sinc`` = sin(pi x)/(pi x) with value 1 at x == 0, in float32;
-  * ``jnp.fft.rfftn`` in complex64 (scipy.fft single precision);
+  * ``jnp.fft.rfftn`` / ``irfftn`` in complex64 / float32 (scipy.fft single
+    precision; irfftn normalised by 1/N like numpy and JAX);
   * ``lax.cond`` / ``lax.scan`` evaluated eagerly.
 """
 from __future__ import annotations
@@ -221,6 +222,7 @@ def _dt(dtype):
 def _build_jnp():
     jnp = types.ModuleType("jax.numpy")
     jnp.pi = np.pi
+    jnp.inf = np.inf
     jnp.int32 = _Caster(np.int32)
     jnp.float32 = _Caster(np.float32)
     jnp.complex64 = _Caster(np.complex64)
@@ -302,7 +304,12 @@ def _build_jnp():
             x = x.astype(np.float32)
         return wrap(scipy.fft.rfftn(x.astype(np.float32), s=s, axes=axes).astype(np.complex64))
 
+    def irfftn(x, s=None, axes=None):
+        x = np.asarray(x).astype(np.complex64)
+        return wrap(scipy.fft.irfftn(x, s=s, axes=axes).astype(np.float32))
+
     fft.rfftn = rfftn
+    fft.irfftn = irfftn
     jnp.fft = fft
     return jnp
 

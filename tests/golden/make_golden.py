@@ -118,6 +118,30 @@ def main(root: str) -> None:
                pipe_edges=edges, pipe_k=np.asarray(k3d, F32), pipe_pk=np.asarray(pk, F32),
                pipe_nmodes=np.asarray(nm, F32))
 
+    # ---- xi_vec (src/correlations.py:120-187) and compute_2pt_correlations (:641-712)
+    xcases = [(16, 100.0, np.arange(0.5, 12.0, 1.0) * 6.25), (12, 60.0, np.linspace(0.0, 40.0, 13)),
+              (32, 1000.0, np.arange(20.0, 600.0, 31.25))]
+    for i, (N, box, s_edges) in enumerate(xcases):
+        s_edges = np.asarray(s_edges, F32)
+        delta = rng.standard_normal((N, N, N)).astype(F32)
+        r3d, xi, nm = corr.xi_vec(delta, box, s_edges)
+        out[f"xi_{i}_delta"] = delta
+        out[f"xi_{i}_box"] = np.array([box], dtype=np.float64)
+        out[f"xi_{i}_sedges"] = s_edges
+        out[f"xi_{i}_r"] = np.asarray(r3d, F32)
+        out[f"xi_{i}_xi"] = np.asarray(xi, F32)
+        out[f"xi_{i}_nmodes"] = np.asarray(nm, F32)
+        kf = 2 * np.pi / box
+        k_edges = np.arange(kf, np.pi * N / box, kf).astype(F32)
+        k3d, pk, nmk, r3d2, xi2 = corr.compute_2pt_correlations(delta, box, s_edges, k_edges)
+        out[f"tpc_{i}_kedges"] = k_edges
+        out[f"tpc_{i}_k"] = np.asarray(k3d, F32)
+        out[f"tpc_{i}_pk"] = np.asarray(pk, F32)
+        out[f"tpc_{i}_nmodes"] = np.asarray(nmk, F32)
+        out[f"tpc_{i}_r"] = np.asarray(r3d2, F32)
+        out[f"tpc_{i}_xi"] = np.asarray(xi2, F32)
+    out["xi_ncases"] = np.array([len(xcases)])
+
     path = os.path.join(HERE, "reference_outputs.npz")
     np.savez_compressed(path, **out)
     print(f"wrote {path} ({os.path.getsize(path) / 1024:.0f} KiB, {len(out)} arrays)")

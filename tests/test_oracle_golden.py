@@ -105,3 +105,20 @@ def test_fast_cpu_stand_in_agrees_with_the_restatement():
     np.testing.assert_allclose(p1[:, 0], p0[:, 0], rtol=1e-4)
     amp = np.abs(p0[:, 0])[:, None]
     assert np.all(np.abs(p1[:, 1:] - p0[:, 1:]) <= 1e-4 * amp)
+
+
+def test_xi_restatement_matches_reference_fixtures(golden):
+    """oracle/reference_f32 xi_vec and compute_2pt_correlations vs the reference's own outputs."""
+    from oracle import reference_f32 as R
+    for i in range(int(golden["xi_ncases"][0])):
+        d, box, se = golden[f"xi_{i}_delta"], float(golden[f"xi_{i}_box"][0]), golden[f"xi_{i}_sedges"]
+        r, xi, nm = R.xi_vec(d, box, se)
+        np.testing.assert_array_equal(r, golden[f"xi_{i}_r"])
+        np.testing.assert_array_equal(nm, golden[f"xi_{i}_nmodes"])
+        np.testing.assert_array_equal(xi, golden[f"xi_{i}_xi"])
+        k, pk, nmk, r2, xi2 = R.compute_2pt_correlations(d, box, se, golden[f"tpc_{i}_kedges"])
+        np.testing.assert_array_equal(k, golden[f"tpc_{i}_k"])
+        np.testing.assert_array_equal(pk, golden[f"tpc_{i}_pk"])
+        np.testing.assert_array_equal(nmk, golden[f"tpc_{i}_nmodes"])
+        np.testing.assert_array_equal(r2, golden[f"tpc_{i}_r"])
+        np.testing.assert_array_equal(xi2, golden[f"tpc_{i}_xi"])
