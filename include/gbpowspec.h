@@ -315,6 +315,22 @@ int gbp_lognormal(int grid, double box, double k_cut, double sigma_v,
  * tests): out = philox(ctr[4], key[2]). */
 int gbp_philox4x32_10(const unsigned* ctr, const unsigned* key, unsigned* out);
 
+/* Two-point correlation multipoles from a density contrast mesh
+ * (src/correlations.py:120-187 xi_vec; the xi half of :641-712
+ * compute_2pt_correlations): forward R2C (plan with one grid), |delta_k|^2
+ * times (sinc)^(-2 mas_order) per axis (the reference: mas_order 2), inverse
+ * C2R into `field` (N^3 floats, unnormalised: N^3 xi), then shells of the
+ * separation r on the full grid with the bin plan's thresholds (edges in
+ * cell units, the jnp.histogram rule) and L_l(mu), mu = r_z / r.
+ * sums_out [nb][3] = sum of field * L_l (double), counts_out [nb] cells per
+ * bin; xi_l = (2l+1) sums / counts / N^6.  mu at r = 0 is NaN when
+ * nan_mu_at_origin (xi_vec: 0/0) and 0 otherwise (compute_2pt). */
+int gbp_xi_workspace_size(gbp_fft_plan plan, gbp_bins bins, size_t* bytes);
+int gbp_xi(gbp_fft_plan plan, const float* delta, void* spectrum, float* field,
+           gbp_bins bins, int mas_order, int nan_mu_at_origin,
+           double* sums_out, long long* counts_out, void* workspace,
+           size_t workspace_bytes, gbp_stream_t stream);
+
 /* ---- Lanes: resident per-mock pipelines for batching and serving --------
  * No reference counterpart (the reference computes one mock per call).
  * A lane owns every buffer one mock needs and, with GBP_LANE_GRAPH, a CUDA

@@ -25,7 +25,8 @@ import torch
 
 from . import _lib, _native
 
-__all__ = ["powspec_vec", "powspec_vec_fundamental", "reference_kedges", "default_kedges"]
+__all__ = ["powspec_vec", "powspec_vec_fundamental", "xi_vec", "compute_2pt_correlations", "reference_kedges",
+           "reference_sedges", "default_kedges"]
 
 _F32 = np.float32
 
@@ -133,3 +134,63 @@ def powspec_vec_fundamental(delta, box_size):
     lastk = torch.from_numpy(_fundamental_last_k(N)).to(d.device)
     k3d = (lastk / nmodes) * float(kf)
     return k3d[1:], pk[1:].to(torch.float32), nmodes[1:]
+
+
+def reference_sedges(s_edges, box_size, n_mesh: int):
+    """Separation edges in cell units as the reference computes them in float32:
+    k_edges = kF * s_edges * dims / box_size, kedges = k_edges / kF (src/correlations.py:124-125,172)."""
+    if isinstance(s_edges, torch.Tensor):
+        s_edges = s_edges.detach().cpu().numpy()
+    box = _box_f32(box_size)
+    kf = _F32(_F32(2.0 * np.pi) / box)
+    se = np.asarray(s_edges, dtype=np.float32).reshape(-1)
+    k_edges = (((kf * se).astype(np.float32) * _F32(n_mesh)).astype(np.float32) / box).astype(np.float32)
+    return (k_edges / kf).astype(np.float32)
+
+
+def _xi(d: torch.Tensor, box: np.float32, s_edges, nan_mu_at_origin: bool):
+    """(r3D, xi3D, Nmodes3D) of a density contrast mesh through gbp_xi."""
+    import ctypes as C
+    N = int(d.shape[0])
+    dev = d.device
+    kedges = reference_sedges(s_edges, box, N)
+    bins = _native.bins_for(kedges, N, dev)
+    plan = _native.fft_plan(N, 1, dev)
+    lib = _lib.load()
+    need = C.c_size_t(0)
+    _lib.check(lib.gbp_xi_workspace_size(plan.handle, bins.handle, C.byref(need)), "gbp_xi_workspace_size")
+    spec = torch.empty(plan.spectrum_floats, dtype=torch.float32, device=dev)
+    field = torch.empty((N, N, N), dtype=torch.float32, device=dev)
+    ws = _native.workspace(need.value, dev)
+    nb = bins.n_bins
+    sums = torch.empty((nb, 3), dtype=torch.float64, device=dev)
+    counts = torch.empty(nb, dtype=torch.int64, device=dev)
+    p = lambda t: C.c_void_p(t.data_ptr())
+    _lib.check(lib.gbp_xi(plan.handle, p(d), p(spec), p(field), bins.handle, 2, int(nan_mu_at_origin), p(sums),
+                          p(counts), p(ws), ws.numel(), _native._stream_of(dev)), "gbp_xi")
+    n3 = float(N) ** 3
+    nm = counts.to(torch.float64)
+    nm = torch.where(nm == 0, torch.full_like(nm, float("inf")), nm)               # :180
+    xi = sums / nm[:, None] / (n3 * n3) * torch.tensor([1.0, 5.0, 9.0], dtype=torch.float64, device=dev)
+    r3d = ((_F32(0.5) * (kedges[1:] + kedges[:-1])) * (box * _F32(1.0) / _F32(N))).astype(np.float32)  # :185
+    return torch.from_numpy(r3d).to(dev), xi.to(torch.float32), nm.to(torch.float32)
+
+
+def xi_vec(delta, box_size, s_edges):
+    """Drop-in for src/correlations.py:120-187 (``xi_vec``): (r3D, xi3D, Nmodes3D).
+
+    |delta_k|^2 with the CIC correction, inverse FFT, separation shells in
+    cell units on the full grid, L_0, L_2, L_4 of mu = r_z / r (NaN at r = 0,
+    as the reference's 0/0), xi_l = (2l+1) sum / N_cells / N^3 (the inverse
+    transform's own 1/N^3 included), empty bins N = inf.
+    """
+    d = _cubic_mesh(delta)
+    return _xi(d, _box_f32(box_size), s_edges, nan_mu_at_origin=True)
+
+
+def compute_2pt_correlations(delta, box_size, s_edges, k_edges):
+    """Drop-in for src/correlations.py:641-712: (k3D, Pk3D, Nmodes3D_pk, r3D, xi3D), mu = 0 at r = 0."""
+    d = _cubic_mesh(delta)
+    k3d, pk, nm = powspec_vec(d, box_size, k_edges)
+    r3d, xi, _ = _xi(d, _box_f32(box_size), s_edges, nan_mu_at_origin=False)
+    return k3d, pk, nm, r3d, xi

@@ -102,3 +102,72 @@ def test_powspec_vec_against_fp64_truth_config1_shape():
     ref = T.power(d.cpu().numpy(), box, (edges / kfe).astype(np.float32), mas_order=2, normalize="none")
     np.testing.assert_array_equal(nm.cpu().numpy().astype(np.int64), ref["nmodes"])
     _assert_pk(pk.cpu().numpy(), ref["pk"], ref["nmodes"])
+
+
+def _assert_xi(got, want, nm):
+    """xi to float32 round-off of the inverse FFT: within 1e-5 of the largest |xi_0| (the r ~ 0 variance)."""
+    got, want = np.asarray(got, np.float64), np.asarray(want, np.float64)
+    scale = np.nanmax(np.abs(want[:, 0]))
+    both_nan = np.isnan(got) & np.isnan(want)
+    assert np.array_equal(np.isnan(got), np.isnan(want))
+    d = np.where(both_nan, 0.0, np.abs(got - want))
+    assert np.all(d <= 1e-5 * scale), (d / scale).max()
+
+
+def test_xi_vec_matches_reference(golden):
+    from gbpowspec import xi_vec
+    for i in range(int(golden["xi_ncases"][0])):
+        d, box, se = golden[f"xi_{i}_delta"], float(golden[f"xi_{i}_box"][0]), golden[f"xi_{i}_sedges"]
+        r, xi, nm = xi_vec(d, box, se)
+        np.testing.assert_array_equal(r.cpu().numpy(), golden[f"xi_{i}_r"])
+        np.testing.assert_array_equal(nm.cpu().numpy(), golden[f"xi_{i}_nmodes"])
+        _assert_xi(xi.cpu().numpy(), golden[f"xi_{i}_xi"], golden[f"xi_{i}_nmodes"])
+
+
+def test_compute_2pt_correlations_matches_reference(golden):
+    from gbpowspec import compute_2pt_correlations
+    for i in range(int(golden["xi_ncases"][0])):
+        d, box, se = golden[f"xi_{i}_delta"], float(golden[f"xi_{i}_box"][0]), golden[f"xi_{i}_sedges"]
+        k, pk, nmk, r, xi = compute_2pt_correlations(d, box, se, golden[f"tpc_{i}_kedges"])
+        np.testing.assert_array_equal(k.cpu().numpy(), golden[f"tpc_{i}_k"])
+        np.testing.assert_array_equal(nmk.cpu().numpy(), golden[f"tpc_{i}_nmodes"])
+        _assert_pk(pk.cpu().numpy(), golden[f"tpc_{i}_pk"], golden[f"tpc_{i}_nmodes"])
+        np.testing.assert_array_equal(r.cpu().numpy(), golden[f"tpc_{i}_r"])
+        _assert_xi(xi.cpu().numpy(), golden[f"tpc_{i}_xi"], None)
+
+
+def test_xi_of_a_large_mesh_against_fp64():
+    """256^3 lognormal contrast: xi_0,2,4 from gbp_xi vs an FP64 numpy evaluation on the same mesh."""
+    from gbpowspec import xi_vec
+    from gbpowspec.synth import lognormal_density
+    N, box = 128, 1000.0
+    d = (lognormal_density(N, box, seed=4) - 1.0).astype(np.float32)
+    se = np.arange(4.0, 200.0, 8.0).astype(np.float32)
+    r, xi, nm = xi_vec(d, box, se)
+    # FP64: same shells, same conventions
+    dk = np.fft.rfftn(d.astype(np.float64))
+    kk = np.fft.fftfreq(N, 1.0 / N)
+    kz = np.arange(N // 2 + 1)
+    w = lambda k: np.sinc(k / N) ** -4
+    p = np.abs(dk) ** 2 * w(kk)[:, None, None] * w(kk)[None, :, None] * w(kz)[None, None, :]
+    field = np.fft.irfftn(p, s=d.shape, axes=(0, 1, 2))
+    ri = np.where(np.arange(N) > N // 2, np.arange(N) - N, np.arange(N))
+    r2 = ri[:, None, None] ** 2 + ri[None, :, None] ** 2 + ri[None, None, :] ** 2
+    rr = np.sqrt(r2.astype(np.float32))
+    from gbpowspec.correlations import reference_sedges
+    e = reference_sedges(se, box, N)
+    idx = np.searchsorted(e, rr.ravel(), side="right")
+    idx = np.where(rr.ravel() == e[-1], e.size - 1, idx)
+    keep = (idx >= 1) & (idx <= e.size - 1)
+    b = idx[keep] - 1
+    with np.errstate(invalid="ignore", divide="ignore"):
+        mu2 = np.where(r2 > 0, (ri[None, None, :] ** 2) / r2, np.nan).ravel()[keep]
+    f = field.ravel()[keep]
+    nb = e.size - 1
+    cnt = np.bincount(b, minlength=nb).astype(np.float64)
+    want = np.stack([np.bincount(b, weights=f, minlength=nb),
+                     5 * np.bincount(b, weights=f * (1.5 * mu2 - 0.5), minlength=nb),
+                     9 * np.bincount(b, weights=f * (35 * mu2 ** 2 - 30 * mu2 + 3) / 8, minlength=nb)], 1)
+    want = want / cnt[:, None] / N ** 3
+    np.testing.assert_array_equal(nm.cpu().numpy(), cnt.astype(np.float32))
+    _assert_xi(xi.cpu().numpy(), want, None)
