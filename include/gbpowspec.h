@@ -331,6 +331,29 @@ int gbp_xi(gbp_fft_plan plan, const float* delta, void* spectrum, float* field,
            double* sums_out, long long* counts_out, void* workspace,
            size_t workspace_bytes, gbp_stream_t stream);
 
+/* ---- Gradients (no C counterpart in the reference, which differentiates
+ * its P(k) with JAX autodiff, tests/lognormal.py:60-103).
+ * gbp_power_backward: given dLoss/dP_l per bin (grad_pk [nb][3], l = 0,2,4),
+ * the spectra of the forward pass (gbp_fft_r2c output, the plan's grids:
+ * 2 = interlaced), the bins' mode counts and the mesh mass (L^3/M^2
+ * normalisation), writes dLoss/d(mesh cell) for every grid (grad_mesh
+ * [G][N^3]).  gbp_deposit_backward: the adjoint of a B-spline deposit
+ * (compat = GBP_COMPAT_NONE): gathers grad_mesh at each particle's stencil
+ * nodes with the weights' derivatives: grad_x/y/z = dLoss/dposition, grad_w
+ * (nullable) = dLoss/dweight through the mesh. */
+int gbp_power_backward_workspace_size(gbp_fft_plan plan, size_t* bytes);
+int gbp_power_backward(const void* spectrum, gbp_fft_plan plan, gbp_bins bins,
+                       int mas_order, const double* grad_pk,
+                       const long long* nmodes, const double* mass,
+                       double box_size, float* grad_mesh, void* workspace,
+                       size_t workspace_bytes, gbp_stream_t stream);
+int gbp_deposit_backward(const float* x, const float* y, const float* z,
+                         const float* w, int64_t n_particles, float xmin,
+                         float ymin, float zmin, float inv_cell, int n_mesh,
+                         int mas, int interlace, const float* grad_mesh,
+                         float* grad_x, float* grad_y, float* grad_z,
+                         float* grad_w, gbp_stream_t stream);
+
 /* ---- Lanes: resident per-mock pipelines for batching and serving --------
  * No reference counterpart (the reference computes one mock per call).
  * A lane owns every buffer one mock needs and, with GBP_LANE_GRAPH, a CUDA

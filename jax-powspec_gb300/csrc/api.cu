@@ -16,7 +16,9 @@
 namespace gbp {
 
 static thread_local cudaError_t g_last_cuda = cudaSuccess;
+static thread_local int g_last_cufft = 0;
 void set_last_cuda_error(cudaError_t e) { g_last_cuda = e; }
+void set_last_cufft_error(int code) { g_last_cufft = code; }
 
 namespace {
 constexpr int LUT_MAX = 2048;
@@ -44,7 +46,11 @@ extern "C" const char* gbp_strerror(int st) {
       snprintf(buf, sizeof(buf), "CUDA error: %s", cudaGetErrorString(g_last_cuda));
       return buf;
     }
-    case GBP_ERR_CUFFT: return "cuFFT error";
+    case GBP_ERR_CUFFT: {
+      static thread_local char buf[64];
+      snprintf(buf, sizeof(buf), "cuFFT error (cufftResult %d)", g_last_cufft);
+      return buf;
+    }
     case GBP_ERR_WORKSPACE: return "workspace too small";
     case GBP_ERR_UNSUPPORTED: return "unsupported configuration";
     case GBP_ERR_ALLOC: return "device allocation failed";

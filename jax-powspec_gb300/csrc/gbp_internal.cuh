@@ -23,6 +23,14 @@
 namespace gbp {
 
 void set_last_cuda_error(cudaError_t e);
+void set_last_cufft_error(int code);   // a cufftResult, reported by gbp_strerror(GBP_ERR_CUFFT)
+
+// Evaluates a cuFFT call; on failure records its result and returns GBP_ERR_CUFFT.
+#define GBP_CUFFT_TRY(expr)                                  \
+  do {                                                       \
+    const int r_ = (int)(expr);                              \
+    if (r_ != 0) { gbp::set_last_cufft_error(r_); return GBP_ERR_CUFFT; } \
+  } while (0)
 
 // Records CUDA events around the launches in its scope while tracing is on
 // (gbp_trace_enable); `name` must be a string literal.

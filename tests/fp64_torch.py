@@ -119,3 +119,60 @@ def ngp_counts(x, y, z, N: int, box: float) -> torch.Tensor:
     (fx, _), (fy, _), (fz, _) = (bspline(grid_coords(c, inv), 1, False) for c in (x, y, z))
     idx = (torch.remainder(fx, N) * N + torch.remainder(fy, N)) * N + torch.remainder(fz, N)
     return torch.bincount(idx, minlength=N ** 3)
+
+
+def power_multipoles_autograd(x, y, z, w, *, box: float, N: int, mas: int, interlace: bool, kedges_grid,
+                              shot_noise: bool = True):
+    """The production estimator in float64 with torch autograd end to end (positions and weights),
+    the reference for the GPU gradients.  Grid coordinates u = x * N / L in float64 (the float32
+    rounding of the kernels is below the gradient test's tolerance)."""
+    dev = x.device
+    inv = N / box
+    wt = torch.ones_like(x, dtype=torch.float64) if w is None else w.to(torch.float64)
+    grids = []
+    for half in ([False, True] if interlace else [False]):
+        st = [bspline(c.to(torch.float64) * inv, mas, half) for c in (x, y, z)]
+        (fx, wx), (fy, wy), (fz, wz) = st
+        R = len(wx)
+        mesh = torch.zeros(N ** 3, dtype=torch.float64, device=dev)
+        for a in range(R):
+            ix = torch.remainder(fx + a, N)
+            for b in range(R):
+                iy = torch.remainder(fy + b, N)
+                for c in range(R):
+                    iz = torch.remainder(fz + c, N)
+                    mesh = mesh.index_add(0, (ix * N + iy) * N + iz, wx[a] * wy[b] * wz[c] * wt)
+        grids.append(mesh.view(N, N, N))
+    M = grids[0].sum()
+    F = [torch.fft.rfftn(m) for m in grids]
+    h = N // 2
+    r = torch.arange(N, device=dev)
+    ki = torch.where(r > h, r - N, r)
+    kx, ky, kz = ki.view(-1, 1, 1), ki.view(1, -1, 1), ki[: h + 1].abs().view(1, 1, -1)
+    if interlace:
+        ph = torch.exp(1j * math.pi * (kx + ky + kz).to(torch.float64) / N)
+        D = 0.5 * (F[0] + F[1] * ph)
+    else:
+        D = F[0]
+    win = lambda k: torch.sinc(k.to(torch.float64) / N) ** (-2 * mas)
+    p = (D.real ** 2 + D.imag ** 2) * win(kx) * win(ky) * win(kz)
+    k2 = (kx * kx + ky * ky + kz * kz).expand(p.shape)
+    mu2 = torch.where(k2 > 0, (kz * kz).to(torch.float64) / k2.clamp(min=1).to(torch.float64), torch.zeros_like(p))
+    p = torch.where(k2 == 0, torch.zeros_like(p), p)
+    edges = torch.tensor(np.asarray(kedges_grid, np.float32), device=dev)
+    b = bin_index(k2, edges).reshape(-1)
+    keep = b >= 0
+    bb = b[keep]
+    nb = edges.numel() - 1
+    pf = p.reshape(-1)[keep]
+    mf = mu2.reshape(-1)[keep]
+    sums = []
+    for lg in (torch.ones_like(mf), 1.5 * mf - 0.5, (35 * mf * mf - 30 * mf + 3) / 8):
+        sums.append(torch.zeros(nb, dtype=torch.float64, device=dev).scatter_add(0, bb, pf * lg))
+    nmodes = torch.bincount(bb, minlength=nb).to(torch.float64)
+    norm = box ** 3 / (M * M)
+    pk = torch.stack([s / nmodes * f for s, f in zip(sums, (1.0, 5.0, 9.0))], dim=1) * norm
+    if shot_noise:
+        shot = box ** 3 * (wt * wt).sum() / (M * M)
+        pk = torch.cat([pk[:, :1] - shot, pk[:, 1:]], dim=1)
+    return pk
