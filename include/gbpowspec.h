@@ -331,6 +331,24 @@ int gbp_xi(gbp_fft_plan plan, const float* delta, void* spectrum, float* field,
            double* sums_out, long long* counts_out, void* workspace,
            size_t workspace_bytes, gbp_stream_t stream);
 
+/* Bispectrum of a density contrast mesh (src/correlations.py:334-462
+ * bispec): shells |k| in [k_i - kF, k_i + kF) around k_1, k_2 and every
+ * k_3(theta), each a run of elementary bins of `bins` (edges in kF units:
+ * the sorted shell limits); shell_bins [n_shells][2] (device) holds the
+ * first and one-past-last elementary bin of shell s (s = 0: k_1, 1: k_2,
+ * 2..: k_3).  Amplitude window sinc^(-mas_order) per axis (the reference:
+ * 2).  Outputs (device, double): pk_out [n_shells] = P of every shell,
+ * bk_out / qk_out [n_shells - 2] = B and the reduced Q per k_3, nmodes_out
+ * [n_shells] (nullable) = modes per shell on the full grid.  The estimator
+ * is the reference's (real-space sums of squares and triple products of
+ * the shell-filtered fields); the sums are evaluated in Fourier space. */
+int gbp_bispec_workspace_size(gbp_fft_plan plan, gbp_bins bins, size_t* bytes);
+int gbp_bispec(gbp_fft_plan plan, const float* delta, void* spectrum,
+               gbp_bins bins, int mas_order, const int32_t* shell_bins,
+               int n_shells, double box_size, double* pk_out, double* bk_out,
+               double* qk_out, long long* nmodes_out, void* workspace,
+               size_t workspace_bytes, gbp_stream_t stream);
+
 /* ---- Gradients (no C counterpart in the reference, which differentiates
  * its P(k) with JAX autodiff, tests/lognormal.py:60-103).
  * gbp_power_backward: given dLoss/dP_l per bin (grad_pk [nb][3], l = 0,2,4),

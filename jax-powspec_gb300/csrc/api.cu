@@ -6,7 +6,10 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <map>
+#include <mutex>
 #include <new>
+#include <tuple>
 #include <vector>
 
 #include "gbp_bins.h"
@@ -19,6 +22,34 @@ static thread_local cudaError_t g_last_cuda = cudaSuccess;
 static thread_local int g_last_cufft = 0;
 void set_last_cuda_error(cudaError_t e) { g_last_cuda = e; }
 void set_last_cufft_error(int code) { g_last_cufft = code; }
+
+int c2r_plan(int N, int P, int batch, cufftHandle* out, size_t* ws) {
+  static std::mutex mu;
+  static std::map<std::tuple<int, int, int, int>, std::pair<cufftHandle, size_t>> cache;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const auto key = std::make_tuple(dev, N, P, batch);
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = cache.find(key);
+  if (it == cache.end()) {
+    cufftHandle h;
+    GBP_CUFFT_TRY(cufftCreate(&h));
+    cufftSetAutoAllocation(h, 0);
+    int n[3] = {N, N, N}, inembed[3] = {N, N, P}, onembed[3] = {N, N, N};
+    size_t w = 0;
+    const int mr =
+        (int)cufftMakePlanMany(h, 3, n, inembed, 1, N * N * P, onembed, 1, N * N * N, CUFFT_C2R, batch, &w);
+    if (mr != 0) {
+      cufftDestroy(h);
+      set_last_cufft_error(mr);
+      return GBP_ERR_CUFFT;
+    }
+    it = cache.emplace(key, std::make_pair(h, w)).first;
+  }
+  *out = it->second.first;
+  *ws = it->second.second;
+  return GBP_OK;
+}
 
 namespace {
 constexpr int LUT_MAX = 2048;

@@ -28,6 +28,11 @@ int own_fft_y(int N, int G, float2* spec, const float2* tw, cudaStream_t st);
 // x pass fused with the binning + the fold into per-bin sums (xbin.cu); spec
 // holds the transform over z and y
 int xbin_power_workspace(gbp_fft_plan plan, gbp_bins bins, int ells, size_t* bytes);
+// Cached cuFFT plan (per device) of `batch` unnormalised inverse real 3-D
+// transforms: complex input rows of P >= N/2+1 entries ([batch][N][N][P]),
+// real output [batch][N][N][N].  No work area of its own: *ws bytes are
+// passed with cufftSetWorkArea (0 when the plan needs none).
+int c2r_plan(int N, int P, int batch, cufftHandle* h, size_t* ws);
 int xbin_power(gbp_fft_plan plan, float2* spec, gbp_bins bins, int mas_order, int ells, const double* mass,
                double* sums_out, long long* nmodes_out, double* ksum_out, void* ws, size_t ws_bytes,
                cudaStream_t st);

@@ -26,10 +26,6 @@
 #include <cufft.h>
 #include <math.h>
 
-#include <map>
-#include <mutex>
-#include <tuple>
-
 #include "gbp_bins.h"
 #include "gbp_fft.h"
 #include "gbp_internal.cuh"
@@ -177,33 +173,6 @@ __global__ void deposit_gather_kernel(const float* __restrict__ x, const float* 
   if (gw) gw[i] = sw;
 }
 
-int grad_c2r_plan(int N, int P, cufftHandle* out, size_t* ws) {
-  static std::mutex mu;
-  static std::map<std::tuple<int, int, int>, std::pair<cufftHandle, size_t>> cache;
-  int dev = 0;
-  cudaGetDevice(&dev);
-  const auto key = std::make_tuple(dev, N, P);
-  std::lock_guard<std::mutex> lock(mu);
-  auto it = cache.find(key);
-  if (it == cache.end()) {
-    cufftHandle h;
-    GBP_CUFFT_TRY(cufftCreate(&h));
-    cufftSetAutoAllocation(h, 0);
-    int n[3] = {N, N, N}, inembed[3] = {N, N, P}, onembed[3] = {N, N, N};
-    size_t w = 0;
-    const int mr = (int)cufftMakePlanMany(h, 3, n, inembed, 1, N * N * P, onembed, 1, N * N * N, CUFFT_C2R, 1, &w);
-    if (mr != 0) {
-      cufftDestroy(h);
-      set_last_cufft_error(mr);
-      return GBP_ERR_CUFFT;
-    }
-    it = cache.emplace(key, std::make_pair(h, w)).first;
-  }
-  *out = it->second.first;
-  *ws = it->second.second;
-  return GBP_OK;
-}
-
 }  // namespace
 }  // namespace gbp
 
@@ -213,7 +182,7 @@ extern "C" int gbp_power_backward_workspace_size(gbp_fft_plan plan, size_t* byte
   if (!plan || !bytes) return GBP_ERR_INVALID;
   cufftHandle h;
   size_t w = 0;
-  const int st = grad_c2r_plan(plan->n, plan->pitch, &h, &w);
+  const int st = c2r_plan(plan->n, plan->pitch, 1, &h, &w);
   if (st) return st;
   *bytes = align256((size_t)plan->grids * plan->n * plan->n * plan->pitch * sizeof(float2)) + align256(w > 0 ? w : 1);
   return GBP_OK;
@@ -229,7 +198,7 @@ extern "C" int gbp_power_backward(const void* spectrum, gbp_fft_plan plan, gbp_b
   const int N = plan->n, P = plan->pitch, G = plan->grids;
   cufftHandle h;
   size_t w = 0;
-  int r = grad_c2r_plan(N, P, &h, &w);
+  int r = c2r_plan(N, P, 1, &h, &w);
   if (r) return r;
   const long long total = (long long)N * N * P;
   const size_t need = align256((size_t)G * total * sizeof(float2)) + align256(w > 0 ? w : 1);

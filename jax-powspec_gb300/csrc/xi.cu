@@ -18,10 +18,6 @@
 #include <cufft.h>
 #include <math.h>
 
-#include <map>
-#include <mutex>
-#include <tuple>
-
 #include "gbp_bins.h"
 #include "gbp_fft.h"
 #include "gbp_internal.cuh"
@@ -132,32 +128,6 @@ struct XiLayout {
   size_t smem, part, c2r_ws, total_ws;
 };
 
-int xi_c2r_plan(int N, int P, cufftHandle* out, size_t* ws) {
-  static std::mutex mu;
-  static std::map<std::tuple<int, int, int>, std::pair<cufftHandle, size_t>> cache;
-  int dev = 0;
-  cudaGetDevice(&dev);
-  const auto key = std::make_tuple(dev, N, P);
-  std::lock_guard<std::mutex> lock(mu);
-  auto it = cache.find(key);
-  if (it == cache.end()) {
-    cufftHandle h;
-    if (cufftCreate(&h) != CUFFT_SUCCESS) return GBP_ERR_CUFFT;
-    cufftSetAutoAllocation(h, 0);
-    int n[3] = {N, N, N}, inembed[3] = {N, N, P}, onembed[3] = {N, N, N};
-    size_t w = 0;
-    if (cufftMakePlanMany(h, 3, n, inembed, 1, N * N * P, onembed, 1, N * N * N, CUFFT_C2R, 1, &w) !=
-        CUFFT_SUCCESS) {
-      cufftDestroy(h);
-      return GBP_ERR_CUFFT;
-    }
-    it = cache.emplace(key, std::make_pair(h, w)).first;
-  }
-  *out = it->second.first;
-  *ws = it->second.second;
-  return GBP_OK;
-}
-
 int xi_layout(const gbp_bins_s* B, int P, size_t r2c_ws, XiLayout& L) {
   const int N = B->N;
   int w = POW_WARPS;
@@ -173,7 +143,7 @@ int xi_layout(const gbp_bins_s* B, int P, size_t r2c_ws, XiLayout& L) {
   L.C = (int)((nw + w - 1) / w);
   L.part = align256((size_t)L.C * XI_NV * B->nbe * sizeof(float2));
   cufftHandle h;
-  int st = xi_c2r_plan(N, P, &h, &L.c2r_ws);
+  int st = c2r_plan(N, P, 1, &h, &L.c2r_ws);
   if (st) return st;
   if (r2c_ws > L.c2r_ws) L.c2r_ws = r2c_ws;          // one work area serves both transforms
   L.total_ws = L.part + align256(L.c2r_ws);
@@ -222,7 +192,7 @@ extern "C" int gbp_xi(gbp_fft_plan plan, const float* delta, void* spectrum, flo
   // 3. inverse real transform (unnormalised)
   cufftHandle h;
   size_t w = 0;
-  r = xi_c2r_plan(N, P, &h, &w);
+  r = c2r_plan(N, P, 1, &h, &w);
   if (r) return r;
   {
     GBP_TRACE("xi_c2r", st);

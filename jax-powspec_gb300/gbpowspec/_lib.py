@@ -120,6 +120,8 @@ SIGNATURES = [
     ("gbp_philox4x32_10", _i, [_vp, _vp, _vp]),
     ("gbp_xi_workspace_size", _i, [_vp, _vp, C.POINTER(_sz)]),
     ("gbp_xi", _i, [_vp, _vp, _vp, _vp, _vp, _i, _i, _vp, _vp, _vp, _sz, _vp]),
+    ("gbp_bispec_workspace_size", _i, [_vp, _vp, C.POINTER(_sz)]),
+    ("gbp_bispec", _i, [_vp, _vp, _vp, _vp, _i, _vp, _i, _d, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     ("gbp_power_backward_workspace_size", _i, [_vp, C.POINTER(_sz)]),
     ("gbp_power_backward", _i, [_vp, _vp, _vp, _i, _vp, _vp, _vp, _d, _vp, _vp, _sz, _vp]),
     ("gbp_deposit_backward", _i, [_vp, _vp, _vp, _vp, _i64, _f, _f, _f, _f, _i, _i, _i, _vp, _vp, _vp, _vp, _vp,

@@ -25,8 +25,8 @@ import torch
 
 from . import _lib, _native
 
-__all__ = ["powspec_vec", "powspec_vec_fundamental", "xi_vec", "compute_2pt_correlations", "reference_kedges",
-           "reference_sedges", "default_kedges"]
+__all__ = ["powspec_vec", "powspec_vec_fundamental", "xi_vec", "compute_2pt_correlations", "bispec", "bispectrum",
+           "bispec_shells", "reference_kedges", "reference_sedges", "default_kedges"]
 
 _F32 = np.float32
 
@@ -194,3 +194,70 @@ def compute_2pt_correlations(delta, box_size, s_edges, k_edges):
     k3d, pk, nm = powspec_vec(d, box_size, k_edges)
     r3d, xi, _ = _xi(d, _box_f32(box_size), s_edges, nan_mu_at_origin=False)
     return k3d, pk, nm, r3d, xi
+
+
+def bispec_shells(box_size, k1, k2, theta):
+    """src/correlations.py:340-358 in float32: k_all = (k1, k2, k3(theta)), k3 = |k1 + k2| at angle theta,
+    and the shell limits (k_all -+ kF) / kF in units of kF.  Returns (k_all, k_min, k_max, theta)."""
+    box = _box_f32(box_size)
+    kF = _F32(_F32(2.0 * np.pi) / box)                                           # :340
+    theta = np.asarray(theta.detach().cpu() if isinstance(theta, torch.Tensor) else theta, dtype=np.float32)
+    if theta.ndim != 1:
+        raise ValueError("theta must be a 1-D array of angles")
+    k1f, k2f = _F32(k1), _F32(k2)
+    k3 = np.sqrt((k2f * np.sin(theta)) ** 2 + (k2f * np.cos(theta) + k1f) ** 2).astype(np.float32)   # :351
+    k_all = np.concatenate([np.array([k1f, k2f], np.float32), k3]).astype(np.float32)               # :352-355
+    return k_all, ((k_all - kF) / kF).astype(np.float32), ((k_all + kF) / kF).astype(np.float32), theta
+
+
+def _elementary_bins(k_min: np.ndarray, k_max: np.ndarray):
+    """Sorted distinct shell limits (+ one edge above them all, so that the closed last bin of the
+    histogram rule is never a shell's) and each shell's [first, one-past-last) elementary bin."""
+    e = np.unique(np.concatenate([k_min, k_max]).astype(np.float32))
+    top = _F32(e[-1] + max(_F32(1.0), abs(e[-1])))
+    edges = np.append(e, top).astype(np.float32)
+    lo = np.searchsorted(edges, k_min, side="left")
+    hi = np.searchsorted(edges, k_max, side="left")
+    return edges, np.stack([lo, hi], axis=1).astype(np.int32)
+
+
+def bispectrum(delta, box_size, k1, k2, theta, *, mas_order: int = 2):
+    """The bispectrum estimator of src/correlations.py:334-462 through gbp_bispec, in double:
+    (k_all [S] float32, P [S], B [S-2], Q [S-2], modes per shell [S]) as CUDA tensors, S = len(theta) + 2."""
+    import ctypes as C
+    d = _cubic_mesh(delta)
+    N = int(d.shape[0])
+    dev = d.device
+    k_all, k_min, k_max, theta_f = bispec_shells(box_size, k1, k2, theta)
+    edges, shell_bins = _elementary_bins(k_min, k_max)
+    bins = _native.bins_for(edges, N, dev)
+    plan = _native.fft_plan(N, 1, dev)
+    lib = _lib.load()
+    need = C.c_size_t(0)
+    _lib.check(lib.gbp_bispec_workspace_size(plan.handle, bins.handle, C.byref(need)), "gbp_bispec_workspace_size")
+    spec = torch.empty(plan.spectrum_floats, dtype=torch.float32, device=dev)
+    ws = _native.workspace(need.value, dev)
+    S = k_all.size
+    sb = torch.from_numpy(shell_bins).to(dev)
+    pk = torch.empty(S, dtype=torch.float64, device=dev)
+    bk = torch.empty(max(S - 2, 1), dtype=torch.float64, device=dev)
+    qk = torch.empty(max(S - 2, 1), dtype=torch.float64, device=dev)
+    nm = torch.empty(S, dtype=torch.int64, device=dev)
+    p = lambda t: C.c_void_p(t.data_ptr())
+    _lib.check(lib.gbp_bispec(plan.handle, p(d), p(spec), bins.handle, int(mas_order), p(sb), S,
+                              float(_box_f32(box_size)), p(pk), p(bk), p(qk), p(nm), p(ws), ws.numel(),
+                              _native._stream_of(dev)), "gbp_bispec")
+    return torch.from_numpy(k_all).to(dev), pk, bk[: S - 2], qk[: S - 2], nm
+
+
+def bispec(delta, box_size, k1, k2, theta):
+    """Drop-in for src/correlations.py:334-462 (``bispec``): (k_all, Pk, theta, B, Q), float32 CUDA tensors.
+
+    Shells [k_i - kF, k_i + kF) around k1, k2 and k3(theta); CIC window on the amplitude; P of every
+    shell, B and the reduced bispectrum Q = B / (P1 P2 + P1 P3 + P2 P3) per angle.
+    """
+    k_all, pk, bk, qk, _ = bispectrum(delta, box_size, k1, k2, theta, mas_order=2)
+    _, _, _, theta_f = bispec_shells(box_size, k1, k2, theta)
+    dev = pk.device
+    return (k_all, pk.to(torch.float32), torch.from_numpy(theta_f).to(dev), bk.to(torch.float32),
+            qk.to(torch.float32))

@@ -46,6 +46,11 @@ def scatter_add(mesh: np.ndarray, idx, vals: np.ndarray) -> None:
     np.add.at(mesh, tuple(a[ok] for a in norm), vals.astype(mesh.dtype)[ok])
 
 
+def _cube(v):
+    """v**3 as lax.integer_pow evaluates it (binary exponentiation): v * (v * v)."""
+    return v * (v * v)
+
+
 def _inv_bin_size(box_size, n_bins):
     bin_size = _f32(box_size) / F32(n_bins)          # src/mas.py:100 (and :17)
     return F32(F32(1.0) / bin_size)                  # src/mas.py:101 (and :18)
@@ -175,7 +180,7 @@ def powspec_vec(delta, box_size, k_edges):
     quad = histogram_f32(kf, kedges, delta2 * (F32(3.0) * mu2 - F32(1.0)) / F32(2.0))       # :46
     hexa = histogram_f32(kf, kedges, delta2 * (F32(35.0) * mu2 * mu2 - F32(30.0) * mu2 + F32(3.0)) / F32(8.0))  # :47
     nmodes = histogram_f32(kf, kedges, None)                                  # :48
-    norm = (_f32(box_size) / F32(dims ** 2)) ** 3
+    norm = _cube(_f32(box_size) / F32(dims ** 2))
     with np.errstate(invalid="ignore", divide="ignore"):
         pk = np.zeros((mono.size, 3), F32)
         pk[:, 0] = mono / nmodes * norm                                       # :50
@@ -272,3 +277,65 @@ def compute_2pt_correlations(delta, box_size, s_edges, k_edges):
     k3d, pk, nm = powspec_vec(delta, box_size, k_edges)
     r3d, xi, _ = _xi_core(delta, box_size, s_edges, mu_zero_at_origin=True)
     return k3d, pk, nm, r3d, xi
+
+
+def bispec_shells(box_size, k1, k2, theta):
+    """src/correlations.py:340-358: k_all = (k1, k2, k3(theta)) and the shell limits in units of kF, float32.
+
+    bispec is jitted, so the box size, k1 and k2 are float32 scalars there; k3 = |k1 + k2| for the angle
+    theta between them.
+    """
+    box = _f32(box_size)
+    kF = F32(F32(2.0 * np.pi) / box)                                           # :340
+    theta = np.asarray(theta, F32)
+    k1f, k2f = _f32(k1), _f32(k2)
+    k3 = np.sqrt((k2f * np.sin(theta)) ** 2 + (k2f * np.cos(theta) + k1f) ** 2).astype(F32)   # :351
+    k_all = np.zeros(theta.size + 2, F32)
+    k_all[0], k_all[1], k_all[2:] = k1f, k2f, k3                              # :352-355
+    k_min = ((k_all - kF) / kF).astype(F32)                                     # :357
+    k_max = ((k_all + kF) / kF).astype(F32)                                     # :358
+    return k_all, k_min, k_max
+
+
+def bispec(delta, box_size, k1, k2, theta):
+    """src/correlations.py:334-462: (k_all, Pk, theta, B, Q), every step in float32.
+
+    delta_i = irfftn(mask_i * W delta_k) and I_i = irfftn(mask_i) per shell (:384-387, :410-413,
+    :427-431); P_i = sum delta_i^2 / sum I_i^2 * (L / N^2)^3 (:396-400, :421-425, :436-441);
+    B = sum delta_1 delta_2 delta_3 / sum I_1 I_2 I_3 * (L^2 / N^3)^3 (:443-449); Q = B / (P1 P2 + P1 P3 +
+    P2 P3) (:450).
+    """
+    delta = np.asarray(delta, F32)
+    dims = delta.shape[0]
+    box = _f32(box_size)
+    theta = np.asarray(theta, F32)
+    k_all, k_min, k_max = bispec_shells(box_size, k1, k2, theta)
+    delta_k = scipy.fft.rfftn(delta, axes=(0, 1, 2)).astype(np.complex64)    # :363
+    kx, ky, kz = _kgrid(dims)
+    corr = _cic_correction(kx, dims) * _cic_correction(ky, dims) * _cic_correction(kz, dims)   # :372
+    delta_k = (delta_k * corr).astype(np.complex64)                           # :373
+    k = np.sqrt((kx * kx + ky * ky + kz * kz).astype(F32))                    # :374
+
+    def fields(i):
+        m = (k >= k_min[i]) & (k < k_max[i])                                  # :379
+        d = scipy.fft.irfftn((m * delta_k).astype(np.complex64), s=delta.shape, axes=(0, 1, 2)).astype(F32)
+        one = scipy.fft.irfftn(m.astype(np.complex64), s=delta.shape, axes=(0, 1, 2)).astype(F32)
+        return d, one
+
+    pnorm = _cube(box / F32(dims ** 2))
+    bnorm = _cube((box * box) / F32(dims ** 3))
+    d1, i1 = fields(0)
+    d2, i2 = fields(1)
+    pk = np.zeros(theta.size + 2, F32)
+    pk[0] = (np.nansum(d1 * d1) / (i1 * i1).sum()) * pnorm                    # :394-400
+    pk[1] = (np.nansum(d2 * d2) / (i2 * i2).sum()) * pnorm                    # :419-425
+    bk = np.zeros(theta.size, F32)
+    qk = np.zeros(theta.size, F32)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        for j in range(theta.size):                                          # the lax.scan of :427-454
+            d3, i3 = fields(j + 2)
+            pv = (np.nansum(d3 * d3) / np.nansum(i3 * i3)) * pnorm
+            bv = (np.nansum(d1 * d2 * d3) / (i1 * i2 * i3).sum()) * bnorm
+            qk[j] = bv / (pk[0] * pk[1] + pk[0] * pv + pk[1] * pv)
+            pk[j + 2], bk[j] = pv, bv
+    return k_all, pk, theta, bk, qk

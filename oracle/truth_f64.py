@@ -152,3 +152,45 @@ def power_multipoles(x, y, z, w, *, box_size: float, n_mesh: int, mas: int, inte
     wt = np.ones(np.asarray(x).size) if w is None else np.asarray(w, F32).astype(np.float64)
     return power(meshes, box_size, kedges_grid, mas_order=mas, normalize="mean",
                  sum_w2=float((wt * wt).sum()) if shot_noise else None)
+
+
+def bispec(delta, box_size, k1, k2, theta, mas_order: int = 2):
+    """The FFT bispectrum estimator of src/correlations.py:334-462 in float64: per shell the
+    inverse transforms of the masked, window-corrected spectrum and of the mask itself, real-space
+    sums of squares and of triple products.  Shell membership is the reference's float32 rule
+    (k = sqrtf(k^2) against float32 limits (k_i -+ kF) / kF), so only the arithmetic differs.
+    The window is sinc^(-p) per axis on the amplitude, p = mas_order (the reference: p = 2).
+    Returns (k_all, P [S], B [S-2], Q [S-2], nmodes [S]) with nmodes counted on the full grid."""
+    F32 = np.float32
+    delta = np.asarray(delta, np.float64)
+    N = delta.shape[0]
+    box = F32(box_size)
+    kF = F32(F32(2.0 * np.pi) / box)
+    theta = np.asarray(theta, F32)
+    k1f, k2f = F32(k1), F32(k2)
+    k3 = np.sqrt((k2f * np.sin(theta)) ** 2 + (k2f * np.cos(theta) + k1f) ** 2).astype(F32)
+    k_all = np.concatenate([[k1f, k2f], k3]).astype(F32)
+    k_min = ((k_all - kF) / kF).astype(F32)
+    k_max = ((k_all + kF) / kF).astype(F32)
+    dk = np.fft.rfftn(delta)
+    r = np.arange(N)
+    ki = np.where(r > N // 2, r - N, r)
+    kx, ky, kz = ki[:, None, None], ki[None, :, None], np.arange(N // 2 + 1)[None, None, :]
+    w = lambda q: np.sinc(q / N) ** (-float(mas_order))
+    dk = dk * w(kx) * w(ky) * w(kz)
+    k = np.sqrt((kx * kx + ky * ky + kz * kz).astype(F32))
+    S = k_all.size
+    d, one, nm = [], [], np.zeros(S, np.int64)
+    for i in range(S):
+        m = (k >= k_min[i]) & (k < k_max[i])
+        d.append(np.fft.irfftn(m * dk, s=delta.shape, axes=(0, 1, 2)))
+        one.append(np.fft.irfftn(m.astype(np.float64), s=delta.shape, axes=(0, 1, 2)))
+        wz = np.where((kz == 0) | ((N % 2 == 0) & (kz == N // 2)), 1, 2)
+        nm[i] = int((np.broadcast_to(m, dk.shape) * wz).sum())
+    L = float(box)
+    pk = np.array([(d[i] ** 2).sum() / (one[i] ** 2).sum() for i in range(S)]) * (L / N ** 2) ** 3
+    with np.errstate(invalid="ignore", divide="ignore"):
+        bk = np.array([(d[0] * d[1] * d[j]).sum() / (one[0] * one[1] * one[j]).sum() for j in range(2, S)])
+        bk = bk * (L * L / N ** 3) ** 3
+        qk = bk / (pk[0] * pk[1] + pk[0] * pk[2:] + pk[1] * pk[2:])
+    return k_all, pk, bk, qk, nm

@@ -255,6 +255,8 @@ def _build_jnp():
 
     jnp.where = where
     jnp.broadcast_to = lambda a, shape: wrap(np.broadcast_to(np.asarray(a), shape))
+    jnp.logical_and = lambda a, b: wrap(np.logical_and(np.asarray(a), np.asarray(b)))
+    jnp.nansum = lambda a: wrap(np.asarray(np.nansum(np.asarray(a))))   # keeps the input's float dtype
 
     def _unary(fn):
         def f(x):

@@ -122,3 +122,42 @@ def test_xi_restatement_matches_reference_fixtures(golden):
         np.testing.assert_array_equal(nmk, golden[f"tpc_{i}_nmodes"])
         np.testing.assert_array_equal(r2, golden[f"tpc_{i}_r"])
         np.testing.assert_array_equal(xi2, golden[f"tpc_{i}_xi"])
+
+
+def test_bispec_restatement_bitexact(golden):
+    """oracle/reference_f32.bispec reproduces the reference's own bispec (src/correlations.py:334-462)."""
+    for i in range(int(golden["bk_ncases"][0])):
+        box, k1, k2 = golden[f"bk_{i}_args"]
+        k, pk, th, bk, qk = R.bispec(golden[f"bk_{i}_delta"], box, k1, k2, golden[f"bk_{i}_theta"])
+        np.testing.assert_array_equal(k, golden[f"bk_{i}_k"])
+        np.testing.assert_array_equal(pk, golden[f"bk_{i}_pk"])
+        np.testing.assert_array_equal(bk, golden[f"bk_{i}_b"])
+        np.testing.assert_array_equal(qk, golden[f"bk_{i}_q"])
+
+
+def test_bispec_truth_f64_matches_reference(golden):
+    """The FP64 bispectrum agrees with the reference's float32 one to float32 round-off."""
+    for i in range(int(golden["bk_ncases"][0])):
+        box, k1, k2 = golden[f"bk_{i}_args"]
+        k, pk, bk, qk, nm = T.bispec(golden[f"bk_{i}_delta"], box, k1, k2, golden[f"bk_{i}_theta"])
+        np.testing.assert_array_equal(k, golden[f"bk_{i}_k"])
+        np.testing.assert_allclose(pk, golden[f"bk_{i}_pk"], rtol=2e-6)
+        np.testing.assert_allclose(bk, golden[f"bk_{i}_b"], rtol=2e-6)
+        np.testing.assert_allclose(qk, golden[f"bk_{i}_q"], rtol=2e-6)
+        assert np.all(nm > 0)
+
+
+def test_bispec_shell_decomposition():
+    """Every shell of the drop-in is a run of elementary bins whose limits are exactly its own."""
+    from gbpowspec.correlations import bispec_shells, _elementary_bins
+    for box, k1, k2, nt in [(100.0, 0.15, 0.25, 6), (300.0, 0.1, 0.1, 7), (2500.0, 0.1, 0.2, 20)]:
+        theta = np.linspace(0, np.pi, nt).astype(np.float32)
+        k_all, kmin, kmax, _ = bispec_shells(box, k1, k2, theta)
+        kr, kminr, kmaxr = R.bispec_shells(box, k1, k2, theta)
+        np.testing.assert_array_equal(k_all, kr)
+        np.testing.assert_array_equal(kmin, kminr)
+        np.testing.assert_array_equal(kmax, kmaxr)
+        edges, sb = _elementary_bins(kmin, kmax)
+        assert np.all(np.diff(edges) > 0) and edges[-1] > max(kmax.max(), kmin.max())
+        np.testing.assert_array_equal(edges[sb[:, 0]], kmin)
+        np.testing.assert_array_equal(edges[sb[:, 1]], kmax)
