@@ -306,6 +306,46 @@ def serving_leg(dev, seed: int, seconds: float = 1.0, rate: float = 200.0) -> di
             "lanes_per_class": 2, "resident_lanes_gb": resident / 1e9}
 
 
+def extensions_leg(dev, seed: int, reps: int = 5) -> dict:
+    """Milliseconds per call (median of `reps` after a warm call, CUDA events) of the estimators beside
+    P_l(k): xi_l(r) of a 256^3 contrast (xi_vec), the bispectrum of a 256^3 contrast at k1 = 0.1, k2 = 0.2,
+    20 angles in [0, pi], L = 2500 (bispec; the reference's tests/bispec.py case), and P_l(k) forward +
+    backward (gradients for 1,048,576 particle positions and weights, 256^3 TSC + interlacing)."""
+    import torch
+    from gbpowspec import bispectrum, power_multipoles_diff, xi_vec
+    from gbpowspec.synth import lognormal_catalogue_gpu, lognormal_density
+    stream = torch.cuda.current_stream(dev)
+
+    def med_ms(fn):
+        fn()
+        torch.cuda.synchronize(dev)
+        ts = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            ts.append(e0.elapsed_time(e1))
+        return float(np.median(ts))
+
+    box = 2500.0
+    d = torch.from_numpy((lognormal_density(256, box, seed=seed) - 1.0).astype(np.float32)).to(dev)
+    s_edges = np.arange(4.0, 200.0, 4.0).astype(np.float32)
+    theta = np.linspace(0.0, np.pi, 20).astype(np.float32)
+    x, y, z = lognormal_catalogue_gpu(1 << 20, box, grid=256, seed=seed, device=dev)
+    w = torch.ones_like(x)
+    pos = [t.clone().requires_grad_(True) for t in (x, y, z, w)]
+
+    def grad_step():
+        pk = power_multipoles_diff(*pos, box_size=box, n_mesh=256, mas="tsc", interlace=True)
+        torch.nan_to_num(pk, nan=0.0).sum().backward()
+
+    return {"xi_vec_256_ms": med_ms(lambda: xi_vec(d, box, s_edges)),
+            "bispec_256_20_angles_ms": med_ms(lambda: bispectrum(d, box, 0.1, 0.2, theta)),
+            "power_grad_256_tsc_interlaced_1M_particles_ms": med_ms(grad_step)}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -320,6 +360,7 @@ def main():
     ap.add_argument("--n-particles", type=int, default=None, help="override the particle count")
     ap.add_argument("--no-covariance", action="store_true", help="skip the batched covariance leg")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving leg")
+    ap.add_argument("--no-extensions", action="store_true", help="skip the xi / bispectrum / gradient timings")
     ap.add_argument("--serve-seconds", type=float, default=1.0)
     ap.add_argument("--profile-only", action="store_true",
                     help="plain path only, warm-up + timed steps (no other legs): a short command for ncu")
@@ -436,6 +477,8 @@ def main():
         extra["batched_covariance"] = covariance_leg(dev, seed=3000 + rank)
     if not args.no_serve:
         extra["serving"] = serving_leg(dev, seed=4000 + rank, seconds=args.serve_seconds)
+    if not args.no_extensions:
+        extra["extensions"] = extensions_leg(dev, seed=5000 + rank)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

@@ -3,13 +3,18 @@
 // deposits).
 //
 // The mesh is never written.  Particles are bucketed (deposit_core.cuh) by
-// column tile: TX x TY pencils (4 x 4; 2 x 4 at 1024^3) spanning the whole z
-// axis, so a stencil is replicated across x and y tile faces only.  One CTA
-// per column tile and grid:
+// column tile: TX x TY pencils (8 x 4 at 256^3 and 512^3, 4 x 4 otherwise)
+// spanning the whole z axis, so a stencil is replicated across x and y tile
+// faces only.  One CTA per column tile and grid:
 //
-//   1. accumulates its bucket in shared memory as exact int64 fixed point
-//      (a native 32-bit atomic on the low word plus a carry into the high
-//      word, as the mesh deposit does),
+//   1. accumulates its bucket in shared memory as 32-bit fixed point with a
+//      scale of its own: 2^s, s = s_g - ceil(log2(c)) (+1 for TSC and PCS,
+//      whose node weights stay below 1/2), where c is the largest number of
+//      the tile's entries covering one z plane (counted first) and 2^s_g
+//      puts the largest particle weight just below 2^30.  No cell can then
+//      exceed 2^30 + rounding in magnitude, whatever the order of the adds,
+//      so the integer sums are exact, order-independent and overflow-free
+//      (fire-and-forget shared reductions, no carries);
 //   2. transforms its pencils along z: the first radix-8 stage reads the
 //      integer cells of two pencils (packed as one complex pencil), converts
 //      them to float and writes the complex buffer that aliases the
@@ -17,7 +22,8 @@
 //   3. splits each packed spectrum into its two real-input half spectra and
 //      writes the pencils' rows of the z-transformed spectrum (P = N/2 + 8
 //      complex per row, as the library's own transform),
-//   4. adds up the tile's exact integer total (the mean density) on the way.
+//   4. adds up the tile's exact integer total, shifted to the common scale
+//      2^s_g (the mean density; stats_kernel folds the tiles).
 //
 // Then the y pass (fft.cu) and the x pass fused with the binning (xbin.cu)
 // finish the transform and the P_l sums.  HBM traffic per grid: the
@@ -33,43 +39,76 @@ namespace {
 
 template <int N>
 struct ColTile {
-  static constexpr int TX = N >= 1024 ? 2 : 4;
+  static constexpr int TX = (N == 256 || N == 512) ? 8 : 4;
   static constexpr int TY = 4;
   static constexpr int NPEN = TX * TY;            // pencils per tile; pencil f = lx * TY + ly
   static constexpr int PAIRS = NPEN / 2;          // complex transforms (pencils 2q, 2q+1)
   static constexpr int NFFT = PAIRS * N / 16;     // butterfly pairs (two columns) per radix-8 stage
   static constexpr int NT = NFFT < 256 ? 256 : NFFT;
-  static constexpr size_t SMEM = (size_t)NPEN * N * 2 * sizeof(unsigned);   // low + high words
+  static constexpr int MINB = NT >= 512 ? 2 : 3;  // CTAs per SM the registers are sized for
+  static constexpr size_t SMEM = (size_t)(NPEN + 1) * N * sizeof(int);   // cells + per-plane entry counts
 };
 
 template <int N, int MAS, int G>
-__global__ void __launch_bounds__(ColTile<N>::NT, 3)
+__global__ void __launch_bounds__(ColTile<N>::NT, ColTile<N>::MINB)
 deposit_fftz_kernel(DepGeom g, const float4* __restrict__ entries, const unsigned* __restrict__ counts,
-                    const unsigned* __restrict__ cursors, const DepCounters* ctr, const float2* __restrict__ tw,
+                    const unsigned* __restrict__ offsets, const DepCounters* ctr, const float2* __restrict__ tw,
                     float2* __restrict__ spec, long long* __restrict__ tile_mass) {
   using CT = ColTile<N>;
   constexpr int R = MAS, TX = CT::TX, TY = CT::TY, NPEN = CT::NPEN, PAIRS = CT::PAIRS, NT = CT::NT;
   constexpr int P = N / 2 + 8, H = N / 2;
-  extern __shared__ __align__(16) unsigned acc32[];
-  unsigned* lo = acc32;                                // [NPEN][N] low words
-  unsigned* hi = acc32 + NPEN * N;                     // [NPEN][N] high words
-  float4* cs4 = reinterpret_cast<float4*>(acc32);      // [PAIRS/2][N] slots of two columns, alias the low words
+  extern __shared__ __align__(16) int acc_smem[];
+  int* acc = acc_smem;                                 // [NPEN][N] fixed-point cells
+  float4* cs4 = reinterpret_cast<float4*>(acc);        // [PAIRS/2][N] slots of two columns, alias the cells
+  int* zc = acc_smem + NPEN * N;                       // [N] entries whose stencil (any grid) covers plane z
   __shared__ long long s_part[NT / 32];
+  __shared__ int s_max[NT / 32];
   const int tid = threadIdx.x;
   const int t = blockIdx.x;
   const int ty = t % g.nt[1], tx = t / g.nt[1];
   const int x0 = tx * TX, y0 = ty * TY;
-  const unsigned end = cursors[t];
-  const unsigned beg = end - counts[t];
-  const int s = fixed_scale_exp(ctr->maxw_bits, 0);
-  const float sc = ldexpf(1.0f, s);
-  const float inv_sc = ldexpf(1.0f, -s);
+  const unsigned beg = offsets[t];
+  const unsigned end = beg + counts[t * CSTRIDE];
+  const int sg = fixed_scale_exp(ctr->maxw_bits, 0);
+  // A cell of plane z only receives entries covering z: the largest such
+  // count bounds every cell of the tile.
+  for (int k = tid; k < N; k += NT) zc[k] = 0;
+  __syncthreads();
+  for (unsigned i = beg + tid; i < end; i += NT) {
+    const float z = entries[i].z;
+    Axis<R> a0;
+    make_axis<MAS, 0>(g, z, 0, a0);
+    int last = a0.first + R - 1;
+    if constexpr (G == 2) {
+      Axis<R> a1;
+      make_axis<MAS, 0>(g, z, 1, a1);
+      last = a1.first + R - 1;                         // a1.first is a0.first or a0.first + 1
+    }
+    for (int zn = a0.first; zn <= last; ++zn) atomicAdd(&zc[wrapn(zn, N)], 1);
+  }
+  __syncthreads();
+  int cmax = 0;
+  for (int k = tid; k < N; k += NT) cmax = max(cmax, zc[k]);
+  cmax = __reduce_max_sync(0xffffffffu, cmax);
+  if ((tid & 31) == 0) s_max[tid >> 5] = cmax;
+  __syncthreads();
+  cmax = 0;
+  for (int k = 0; k < NT / 32; ++k) cmax = max(cmax, s_max[k]);
+  const unsigned cnt = (unsigned)cmax;
+  const int lg = cnt > 1u ? 32 - __clz(cnt - 1u) : 0;  // ceil(log2(entries per plane))
+  // a node weight of TSC (<= 0.75^3) or PCS (<= (2/3)^3) is below 1/2: one more bit
+  constexpr int WBIT = (MAS == GBP_TSC || MAS == GBP_PCS) ? 1 : 0;
+  const int sh = lg > WBIT ? lg - WBIT : 0;            // tile scale 2^s = 2^(sg - sh), never finer than 2^sg
+  const int s = sg - sh;
+  // 2^s and 2^-s as two exact power-of-two factors each (s may reach -130)
+  const float up1 = ldexpf(1.0f, s / 2), up2 = ldexpf(1.0f, s - s / 2);
+  const float dn1 = ldexpf(1.0f, -(s / 2)), dn2 = ldexpf(1.0f, -(s - s / 2));
   const long long gstride = (long long)N * N * P;
 
   for (int grid = 0; grid < G; ++grid) {
     {
-      uint4* a4 = reinterpret_cast<uint4*>(acc32);
-      for (int k = tid; k < 2 * NPEN * N / 4; k += NT) a4[k] = make_uint4(0u, 0u, 0u, 0u);
+      uint4* a4 = reinterpret_cast<uint4*>(acc);
+      for (int k = tid; k < NPEN * N / 4; k += NT) a4[k] = make_uint4(0u, 0u, 0u, 0u);
     }
     __syncthreads();
     for (unsigned i = beg + tid; i < end; i += NT) {
@@ -81,7 +120,7 @@ deposit_fftz_kernel(DepGeom g, const float4* __restrict__ entries, const unsigne
       int lx[R], ly[R], zz[R];
       local_nodes<R>(ax, N, x0, TX, lx);
       local_nodes<R>(ay, N, y0, TY, ly);
-      const float wsc = __fmul_rn(e.w, sc);                 // exact: sc is a power of two
+      const float wsc = __fmul_rn(__fmul_rn(e.w, up1), up2);   // exact: powers of two
       float wz[R];
 #pragma unroll
       for (int r = 0; r < R; ++r) {
@@ -96,19 +135,8 @@ deposit_fftz_kernel(DepGeom g, const float4* __restrict__ entries, const unsigne
           if (ly[ry] < 0) continue;
           const float wxy = __fmul_rn(ax.w[rx], ay.w[ry]);
           const int row = (lx[rx] * TY + ly[ry]) * N;
-          int q[R];
-          unsigned old[R];
 #pragma unroll
-          for (int rz = 0; rz < R; ++rz) {                 // the pencil's low-word adds together
-            q[rz] = __float2int_rn(__fmul_rn(wxy, wz[rz]));
-            old[rz] = atomicAdd(&lo[row + zz[rz]], static_cast<unsigned>(q[rz]));
-          }
-#pragma unroll
-          for (int rz = 0; rz < R; ++rz) {                 // then the carries into the high words
-            const unsigned add = static_cast<unsigned>(q[rz]);
-            const int dh = (q[rz] < 0 ? -1 : 0) + (old[rz] + add < old[rz] ? 1 : 0);
-            if (dh) atomicAdd(&hi[row + zz[rz]], static_cast<unsigned>(dh));
-          }
+          for (int rz = 0; rz < R; ++rz) atomicAdd(&acc[row + zz[rz]], __float2int_rn(__fmul_rn(wxy, wz[rz])));
         }
       }
     }
@@ -117,14 +145,13 @@ deposit_fftz_kernel(DepGeom g, const float4* __restrict__ entries, const unsigne
     // z transform: pencils 2q and 2q+1 are the real and imaginary parts of
     // column q; a thread transforms columns 2cp and 2cp+1 (pencils 4cp..4cp+3)
     long long part = 0;
-    auto gin = [&part, inv_sc, lo, hi](int j, int cp) {
+    auto gin = [&part, dn1, dn2, acc](int j, int cp) {
       float v[4];
 #pragma unroll
       for (int f = 0; f < 4; ++f) {
-        const int c = (4 * cp + f) * N + j;
-        const long long a = (long long)(((unsigned long long)hi[c] << 32) | lo[c]);
-        part += a;
-        v[f] = fixed_to_float(a, inv_sc);
+        const int q = acc[(4 * cp + f) * N + j];
+        part += q;
+        v[f] = __fmul_rn(__fmul_rn(__int2float_rn(q), dn1), dn2);
       }
       return make_float4(v[0], v[1], v[2], v[3]);
     };
@@ -153,14 +180,14 @@ deposit_fftz_kernel(DepGeom g, const float4* __restrict__ entries, const unsigne
       __stcs(out + r1 * P + k, b);
     }
 
-    // this tile's exact total (read by stats_kernel)
+    // this tile's exact total at the common scale 2^sg (read by stats_kernel)
     for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
     if ((tid & 31) == 0) s_part[tid >> 5] = part;
     __syncthreads();                                   // also: the next grid reuses the accumulators
     if (tid == 0) {
       long long tm = 0;
       for (int k = 0; k < NT / 32; ++k) tm += s_part[k];
-      tile_mass[(long long)grid * gridDim.x + t] = tm;
+      tile_mass[(long long)grid * gridDim.x + t] = tm * (1LL << sh);   // exact, at the common scale 2^sg
     }
   }
 }
@@ -211,7 +238,7 @@ int run_fused(const DepGeom& g, const DepLayout& L, const DepBuffers& b, const f
   const size_t smem = ColTile<N>::SMEM;
   GBP_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   GBP_TRACE("deposit_fft_z", st);
-  k<<<L.ntiles, ColTile<N>::NT, smem, st>>>(g, b.entries, b.counts, b.cursors, b.ctr, tw, spec, b.tile_mass);
+  k<<<L.ntiles, ColTile<N>::NT, smem, st>>>(g, b.entries, b.counts, b.offsets, b.ctr, tw, spec, b.tile_mass);
   GBP_LAUNCH_CHECK();
   return GBP_OK;
 }
@@ -250,7 +277,7 @@ int particles_power(DepGeom g, int64_t n_launch, gbp_fft_plan plan, gbp_bins B, 
   g.vec_ok = 0;
   const int N = B->N, G = plan->grids;
   float2* spec = static_cast<float2*>(spectrum);
-  GBP_CUDA_TRY(cudaMemsetAsync(b.ctr, 0, align256(sizeof(DepCounters)) + align256((size_t)L.dep.ntiles * 4), st));
+  GBP_CUDA_TRY(cudaMemsetAsync(b.ctr, 0, zeroed_bytes(L.dep), st));
   switch (N) {
     case 64: r = dispatch_fused<64>(mas, G, g, L.dep, b, plan->tw, spec, st); break;
     case 128: r = dispatch_fused<128>(mas, G, g, L.dep, b, plan->tw, spec, st); break;

@@ -6,10 +6,11 @@
 //                      that its stencil touches (integer atomics: the counts
 //                      do not depend on order), and reduces max|w|, sum w and
 //                      sum w^2 per block.
-//   2. cub scan        exclusive prefix sum of the tile counts -> cursors.
+//   2. cub scan        exclusive prefix sum of the tile counts -> offsets.
 //   3. scatter_kernel  every particle appends (u_x, u_y, u_z, w) to each
 //                      touched tile's bucket: a one-digit radix sort of the
 //                      particles by tile, replicated across tile faces.
+//                      (Per-tile counters sit one L2 line apart.)
 //   4. deposit_kernel  one CTA per tile accumulates its bucket in shared
 //                      memory in int64 fixed point (scale 2^s fixed by max|w|;
 //                      each add is a native 32-bit atomic on the low word plus
@@ -38,7 +39,7 @@ namespace {
 template <int MAS, int G, int CM>
 __global__ void __launch_bounds__(DEP_THREADS)
 deposit_kernel(DepGeom g, const float4* __restrict__ entries, const unsigned* __restrict__ counts,
-               const unsigned* __restrict__ cursors, const DepCounters* ctr, const float* __restrict__ mesh_in,
+               const unsigned* __restrict__ offsets, const DepCounters* ctr, const float* __restrict__ mesh_in,
                float* __restrict__ mesh_out, long long* __restrict__ tile_mass) {
   constexpr int R = Scheme<MAS, CM>::R;
   extern __shared__ __align__(16) unsigned acc32[];
@@ -50,8 +51,8 @@ deposit_kernel(DepGeom g, const float4* __restrict__ entries, const unsigned* __
   const int x0 = tx * g.td[0], y0 = ty * g.td[1], z0 = tz * g.td[2];
   const int ex = min(g.td[0], g.N - x0), ey = min(g.td[1], g.N - y0), ez = min(g.td[2], g.N - z0);
 
-  const unsigned end = cursors[t];
-  const unsigned beg = end - counts[t];
+  const unsigned beg = offsets[t];
+  const unsigned end = beg + counts[t * CSTRIDE];
   const int s = fixed_scale_exp(ctr->maxw_bits, CM);
   const float sc = ldexpf(1.0f, s);
   const float inv_sc = ldexpf(1.0f, -s);
@@ -165,7 +166,7 @@ int run_scheme(const DepGeom& g, const DepLayout& L, const DepBuffers& b, const 
   GBP_CUDA_TRY(cudaFuncSetAttribute(deposit_kernel<MAS, G, CM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)smem));
   GBP_TRACE("deposit_tiles", st);
-  deposit_kernel<MAS, G, CM><<<L.ntiles, DEP_THREADS, smem, st>>>(g, b.entries, b.counts, b.cursors, b.ctr, mesh_in,
+  deposit_kernel<MAS, G, CM><<<L.ntiles, DEP_THREADS, smem, st>>>(g, b.entries, b.counts, b.offsets, b.ctr, mesh_in,
                                                                  mesh_out, b.tile_mass);
   GBP_LAUNCH_CHECK();
   return GBP_OK;
@@ -178,8 +179,7 @@ int deposit_launch(DepGeom g, const DepLayout& L, int64_t n, int mas, int G, int
   const DepBuffers b = carve_deposit(workspace, L, n);
   for (int a = 0; a < 3; ++a) { g.td[a] = L.td[a]; g.ts[a] = L.ts[a]; g.nt[a] = L.nt[a]; }
   g.vec_ok = ((reinterpret_cast<uintptr_t>(mesh_out) | reinterpret_cast<uintptr_t>(mesh_in)) & 15u) == 0;
-  // counters + tile counts are adjacent: one memset clears both.
-  GBP_CUDA_TRY(cudaMemsetAsync(b.ctr, 0, align256(sizeof(DepCounters)) + align256((size_t)L.ntiles * 4), stream));
+  GBP_CUDA_TRY(cudaMemsetAsync(b.ctr, 0, zeroed_bytes(L), stream));
   int st;
   if (compat == GBP_COMPAT_VEC) st = run_scheme<GBP_CIC, 1, GBP_COMPAT_VEC>(g, L, b, mesh_in, mesh_out, stream);
   else if (compat == GBP_COMPAT_SCAN) st = run_scheme<GBP_CIC, 1, GBP_COMPAT_SCAN>(g, L, b, mesh_in, mesh_out, stream);

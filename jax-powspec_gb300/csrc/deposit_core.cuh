@@ -5,6 +5,8 @@
 #pragma once
 
 #include <cub/device/device_scan.cuh>
+#include <thrust/iterator/counting_iterator.h>
+#include <thrust/iterator/transform_iterator.h>
 
 #include "gbp_internal.cuh"
 
@@ -18,6 +20,9 @@ constexpr int CNT_THREADS = 256;
 constexpr int CNT_ITEMS = 2;          // particles per thread in count/scatter
 constexpr float MAX_ABS_U = 1073741824.0f;  // |u| < 2^30 cells, else dropped
 constexpr int kCubeTiles[3] = {TILE, TILE, TILE};   // mesh deposit: 16^3-cell tiles
+// Per-tile counters sit one 128-byte line apart: the bucketing's global
+// atomics on different tiles never contend for one L2 line.
+constexpr int CSTRIDE = 32;
 
 struct DepGeom {
   const float* x;
@@ -262,8 +267,8 @@ count_kernel(DepGeom gp, unsigned* __restrict__ counts, DepCounters* ctr, float4
     for (int a = 0; a < nx; ++a)
       for (int b = 0; b < ny; ++b)
         for (int c = 0; c < nz; ++c)
-          atomicAdd(&counts[(pick3(a, x0, x1, x2) * g.nt[1] + pick3(b, y0, y1, y2)) * g.nt[2] + pick3(c, z0, z1, z2)],
-                    1u);
+          atomicAdd(&counts[((pick3(a, x0, x1, x2) * g.nt[1] + pick3(b, y0, y1, y2)) * g.nt[2] +
+                             pick3(c, z0, z1, z2)) * CSTRIDE], 1u);
     maxw = fmaxf(maxw, fabsf(w));
     sw = ff_add_f(sw, w);
     sw2 = ff_add_f(sw2, __fmul_rn(w, w));
@@ -299,7 +304,8 @@ count_kernel(DepGeom gp, unsigned* __restrict__ counts, DepCounters* ctr, float4
 // Pass 3: append (u_x, u_y, u_z, w) to every touched tile's bucket.
 template <int MAS, int G, int CM>
 __global__ void __launch_bounds__(CNT_THREADS)
-scatter_kernel(DepGeom gp, unsigned* __restrict__ cursors, float4* __restrict__ entries) {
+scatter_kernel(DepGeom gp, const unsigned* __restrict__ offsets, unsigned* __restrict__ fills,
+               float4* __restrict__ entries) {
   DepGeom g = gp;
   resolve_job(g);
   Batch bt;
@@ -320,7 +326,7 @@ scatter_kernel(DepGeom gp, unsigned* __restrict__ cursors, float4* __restrict__ 
       for (int b = 0; b < ny; ++b)
         for (int c = 0; c < nz; ++c) {
           const int t = (pick3(a, x0, x1, x2) * g.nt[1] + pick3(b, y0, y1, y2)) * g.nt[2] + pick3(c, z0, z1, z2);
-          entries[atomicAdd(&cursors[t], 1u)] = e;
+          entries[offsets[t] + atomicAdd(&fills[t * CSTRIDE], 1u)] = e;
         }
   }
 }
@@ -422,6 +428,21 @@ struct DepLayout {
   size_t total;
 };
 
+// Bytes at the start of the workspace that one memset clears per call: the
+// counters, the tiles' entry counts and their fill counters (adjacent).
+inline size_t zeroed_bytes(const DepLayout& L) {
+  return align256(sizeof(DepCounters)) + 2 * align256((size_t)L.ntiles * CSTRIDE * sizeof(unsigned));
+}
+
+struct StrideLoad {
+  const unsigned* p;
+  __host__ __device__ unsigned operator()(int i) const { return p[(long long)i * CSTRIDE]; }
+};
+
+inline thrust::transform_iterator<StrideLoad, thrust::counting_iterator<int>> strided_counts(const unsigned* p) {
+  return thrust::make_transform_iterator(thrust::counting_iterator<int>(0), StrideLoad{p});
+}
+
 // Largest number of distinct tiles a run of `width` consecutive nodes can
 // touch along one periodic axis (exact, by enumeration).
 int max_tiles_axis(int N, int tdim, int width) {
@@ -463,9 +484,9 @@ int deposit_layout(int64_t n, int N, int mas, int interlace, int compat, const i
   if ((double)n * L.maxrep >= 4294967295.0) return GBP_ERR_UNSUPPORTED;
   L.nblocks = (int)((n + (long long)CNT_THREADS * CNT_ITEMS - 1) / ((long long)CNT_THREADS * CNT_ITEMS));
   L.scan_bytes = 0;
-  cub::DeviceScan::ExclusiveSum(nullptr, L.scan_bytes, (unsigned*)nullptr, (unsigned*)nullptr, L.ntiles);
+  cub::DeviceScan::ExclusiveSum(nullptr, L.scan_bytes, strided_counts(nullptr), (unsigned*)nullptr, L.ntiles);
   const size_t nbl = (size_t)(L.nblocks > 0 ? L.nblocks : 1);
-  L.total = align256(sizeof(DepCounters)) + align256((size_t)L.ntiles * 4) * 2 + align256(nbl * sizeof(float4)) +
+  L.total = zeroed_bytes(L) + align256((size_t)L.ntiles * 4) + align256(nbl * sizeof(float4)) +
             align256(nbl * sizeof(uint2)) + align256((size_t)L.ntiles * 2 * sizeof(long long)) +
             align256((size_t)n * L.maxrep * sizeof(float4) + 16) + align256(L.scan_bytes);
   return GBP_OK;
@@ -474,8 +495,9 @@ int deposit_layout(int64_t n, int N, int mas, int interlace, int compat, const i
 // Workspace slices shared by both deposit paths.
 struct DepBuffers {
   DepCounters* ctr;
-  unsigned* counts;
-  unsigned* cursors;
+  unsigned* counts;      // [ntiles * CSTRIDE] entries per tile (count pass)
+  unsigned* fills;       // [ntiles * CSTRIDE] entries written so far (scatter pass)
+  unsigned* offsets;     // [ntiles] first entry of each tile (exclusive scan of the counts)
   float4* block_stats;
   uint2* block_counts;
   long long* tile_mass;
@@ -488,8 +510,9 @@ inline DepBuffers carve_deposit(void* workspace, const DepLayout& L, int64_t n) 
   DepBuffers b;
   const int nbl = L.nblocks > 0 ? L.nblocks : 1;
   b.ctr = cv.take<DepCounters>(1);
-  b.counts = cv.take<unsigned>(L.ntiles);
-  b.cursors = cv.take<unsigned>(L.ntiles);
+  b.counts = cv.take<unsigned>((size_t)L.ntiles * CSTRIDE);
+  b.fills = cv.take<unsigned>((size_t)L.ntiles * CSTRIDE);
+  b.offsets = cv.take<unsigned>(L.ntiles);
   b.block_stats = cv.take<float4>(nbl);
   b.block_counts = cv.take<uint2>(nbl);
   b.tile_mass = cv.take<long long>((size_t)L.ntiles * 2);
@@ -498,8 +521,8 @@ inline DepBuffers carve_deposit(void* workspace, const DepLayout& L, int64_t n) 
   return b;
 }
 
-// Passes 1-3: bucket the particles by tile (counters and tile counts must
-// be zero on entry).
+// Passes 1-3: bucket the particles by tile (the first zeroed_bytes(L) of the
+// workspace must be zero on entry).
 template <int MAS, int G, int CM>
 int bucket_particles(const DepGeom& g, const DepLayout& L, const DepBuffers& b, cudaStream_t st) {
   if (L.nblocks > 0) {
@@ -510,11 +533,12 @@ int bucket_particles(const DepGeom& g, const DepLayout& L, const DepBuffers& b, 
   {
     GBP_TRACE("deposit_scan", st);
     size_t scan_bytes = L.scan_bytes;
-    GBP_CUDA_TRY(cub::DeviceScan::ExclusiveSum(b.scan_tmp, scan_bytes, b.counts, b.cursors, L.ntiles, st));
+    GBP_CUDA_TRY(cub::DeviceScan::ExclusiveSum(b.scan_tmp, scan_bytes, strided_counts(b.counts), b.offsets,
+                                               L.ntiles, st));
   }
   if (L.nblocks > 0) {
     GBP_TRACE("deposit_scatter", st);
-    scatter_kernel<MAS, G, CM><<<L.nblocks, CNT_THREADS, 0, st>>>(g, b.cursors, b.entries);
+    scatter_kernel<MAS, G, CM><<<L.nblocks, CNT_THREADS, 0, st>>>(g, b.offsets, b.fills, b.entries);
     GBP_LAUNCH_CHECK();
   }
   return GBP_OK;

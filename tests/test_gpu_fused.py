@@ -122,7 +122,10 @@ def test_particles_power_matches_mesh_path(N, mas, G):
     assert torch.equal(got.ksum, want.ksum)
     a, b = read_stats(st), read_stats(st_mesh)
     assert a.n_kept == b.n_kept == x.numel()
-    np.testing.assert_allclose(a.mass[:G], b.mass[:G], rtol=1e-9)
+    # both totals are exact sums of their meshes' fixed-point cells; the fused tiles quantise each
+    # contribution at ~2^-(s_g - log2 entries) (about 2^-18 of the largest weight here) instead of 2^-s_g,
+    # and stencil tails below half a step round to zero: the fused mass is ~2e-7 low
+    np.testing.assert_allclose(a.mass[:G], b.mass[:G], rtol=1e-6)
     wv, gv = want.sums.cpu().numpy(), got.sums.cpu().numpy()
     amp = np.abs(wv[:, 0])
     for l in range(3):
