@@ -157,7 +157,12 @@ deposit_fftz_kernel(DepGeom g, const float4* __restrict__ entries, const unsigne
     };
     auto sin_ = [cs4](int j, int cp) { return cs4[cp * N + fft::zsw(j)]; };
     auto sout = [cs4](int j, int cp, float4 v) { cs4[cp * N + fft::zsw(j)] = v; };
-    fft::run_stages2<N, PAIRS / 2, NT, true, true, true>(gin, sin_, sout, sout, tw, tid);
+    // N = 512: every stage is radix 8 and the 64 threads of a column pair own
+    // its data (the first stage's writes alias the pair's own pencils), so
+    // the stages synchronise 64-thread groups only
+    constexpr int GS = (N == 512 && NT == PAIRS / 2 * (N / 8)) ? N / 8 : 0;
+    fft::run_stages2<N, PAIRS / 2, NT, true, true, true, decltype(gin), decltype(sin_), decltype(sout),
+                     decltype(sout), GS>(gin, sin_, sout, sout, tw, tid);
 
     // split the packed spectra; write all pencils' rows (row padding -> 0)
     const float2* cs = reinterpret_cast<const float2*>(cs4);

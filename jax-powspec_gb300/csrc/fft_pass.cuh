@@ -48,12 +48,27 @@ __device__ __forceinline__ float2 lo2(float4 v) { return make_float2(v.x, v.y); 
 __device__ __forceinline__ float2 hi2(float4 v) { return make_float2(v.z, v.w); }
 __device__ __forceinline__ float4 pack2(float2 a, float2 b) { return make_float4(a.x, a.y, b.x, b.y); }
 
+// Barrier of the GS consecutive threads that share data (a named barrier,
+// id 1 + tid / GS), or of the whole CTA when GS == 0.
+template <int GS>
+__device__ __forceinline__ void group_sync(int tid) {
+  if constexpr (GS == 0) {
+    __syncthreads();
+  } else {
+    static_assert(GS % 32 == 0, "named barriers count whole warps");
+    asm volatile("bar.sync %0, %1;" ::"r"(1 + tid / GS), "n"(GS) : "memory");
+  }
+}
+
 // One stage over CP column pairs.  In(row, cp) -> float4, Out(row, cp, float4).
 // MID_SYNC separates the reads from the writes (in-place shared stages);
 // END_SYNC publishes the writes.  IFAST: thread b owns butterfly b % (N/R) of
 // column pair b / (N/R) (consecutive lanes, consecutive rows); otherwise
-// column pair b % CP, butterfly b / CP.
-template <int N, int R, int CP, int NT, bool MID_SYNC, bool END_SYNC, bool IFAST, class In, class Out>
+// column pair b % CP, butterfly b / CP.  GS > 0 (IFAST, N/R == GS threads per
+// column pair, one butterfly each): the barriers cover only the threads of
+// one column pair, whose data no other thread touches.
+template <int N, int R, int CP, int NT, bool MID_SYNC, bool END_SYNC, bool IFAST, class In, class Out,
+          int GS = 0>
 __device__ __forceinline__ void stage2(In in, Out out, const float2* __restrict__ tw, int p, int tid) {
   constexpr int NB = CP * (N / R);
   constexpr int PER = (NB + NT - 1) / NT;
@@ -98,7 +113,8 @@ __device__ __forceinline__ void stage2(In in, Out out, const float2* __restrict_
 #pragma unroll
     for (int r = 0; r < R; ++r) u[q][r] = pack2(a[r], c[r]);
   }
-  if (MID_SYNC) __syncthreads();
+  static_assert(GS == 0 || (IFAST && N / R == GS && NB == NT), "group barriers need one column pair per group");
+  if (MID_SYNC) group_sync<GS>(tid);
 #pragma unroll
   for (int q = 0; q < PER; ++q) {
     const int b = tid + q * NT;
@@ -109,7 +125,7 @@ __device__ __forceinline__ void stage2(In in, Out out, const float2* __restrict_
 #pragma unroll
     for (int r = 0; r < R; ++r) out(j + r * p, cp, u[q][r]);
   }
-  if (END_SYNC) __syncthreads();
+  if (END_SYNC) group_sync<GS>(tid);
 }
 
 // Full transform: the first stage reads `gin`, the stages in between go
@@ -120,20 +136,23 @@ __device__ __forceinline__ void stage2(In in, Out out, const float2* __restrict_
 // reads (each then reads everything before it writes; OUT_SHARED also ends
 // with a barrier).
 template <int N, int CP, int NT, bool IFAST, bool IN_SHARED, bool OUT_SHARED, class GIn, class SIn, class SOut,
-          class GOut>
+          class GOut, int GS = 0>
 __device__ __forceinline__ void run_stages2(GIn gin, SIn sin_, SOut sout, GOut gout, const float2* __restrict__ tw,
                                             int tid) {
   using RD = Radices<N>;
   static_assert(RD::stages >= 2, "at least two stages");
-  stage2<N, 8, CP, NT, IN_SHARED, true, IFAST>(gin, sout, tw, 1, tid);
+  static_assert(GS == 0 || RD::tail == 0, "group barriers need radix-8 stages only");
+  stage2<N, 8, CP, NT, IN_SHARED, true, IFAST, GIn, SOut, GS>(gin, sout, tw, 1, tid);
   int p = 8;
   if constexpr (RD::tail == 0) {
 #pragma unroll
     for (int st = 1; st < RD::n8 - 1; ++st) {
-      stage2<N, 8, CP, NT, true, true, IFAST>(sin_, sout, tw, p, tid);
+      stage2<N, 8, CP, NT, true, true, IFAST, SIn, SOut, GS>(sin_, sout, tw, p, tid);
       p *= 8;
     }
-    stage2<N, 8, CP, NT, OUT_SHARED, OUT_SHARED, IFAST>(sin_, gout, tw, p, tid);
+    // the last stage's outputs may be read by any thread: a CTA barrier ends it
+    stage2<N, 8, CP, NT, OUT_SHARED, false, IFAST, SIn, GOut, GS>(sin_, gout, tw, p, tid);
+    if (OUT_SHARED) __syncthreads();
   } else {
 #pragma unroll
     for (int st = 1; st < RD::n8; ++st) {
