@@ -15,14 +15,14 @@ from ._lib import GbpError, DepositStats, load as load_library
 from ._native import read_stats
 from .mas import cic_mas, cic_mas_vec, mesh_deposit
 from .correlations import (powspec_vec, powspec_vec_fundamental, xi_vec, compute_2pt_correlations, bispec, bispectrum,
-                           default_kedges)
+                           compute_all_correlations, default_kedges)
 from .pipeline import PkConfig, PkResult, PowerSpectrum, power_multipoles, algorithmic_bytes
 from .grad import power_multipoles_diff
 
 __all__ = [
     "GbpError", "DepositStats", "load_library", "read_stats",
     "cic_mas", "cic_mas_vec", "mesh_deposit",
-    "powspec_vec", "powspec_vec_fundamental", "xi_vec", "compute_2pt_correlations", "bispec", "bispectrum",
+    "powspec_vec", "powspec_vec_fundamental", "xi_vec", "compute_2pt_correlations", "bispec", "bispectrum", "compute_all_correlations",
     "default_kedges",
     "PkConfig", "PkResult", "PowerSpectrum", "power_multipoles", "algorithmic_bytes", "power_multipoles_diff",
 ]

@@ -26,7 +26,7 @@ import torch
 from . import _lib, _native
 
 __all__ = ["powspec_vec", "powspec_vec_fundamental", "xi_vec", "compute_2pt_correlations", "bispec", "bispectrum",
-           "bispec_shells", "reference_kedges", "reference_sedges", "default_kedges"]
+           "compute_all_correlations", "bispec_shells", "reference_kedges", "reference_sedges", "default_kedges"]
 
 _F32 = np.float32
 
@@ -261,3 +261,18 @@ def bispec(delta, box_size, k1, k2, theta):
     dev = pk.device
     return (k_all, pk.to(torch.float32), torch.from_numpy(theta_f).to(dev), bk.to(torch.float32),
             qk.to(torch.float32))
+
+
+def compute_all_correlations(delta, box_size, s_edges, k_edges, k1, k2, theta):
+    """Drop-in for src/correlations.py:464-637: (k3D, Pk3D, Nmodes3D_pk, r3D, xi3D, Nmodes3D_xi, k_all, Pk,
+    theta, B, Q), float32 CUDA tensors.
+
+    P_l(k) and xi_l(r) as ``compute_2pt_correlations`` (mu = 0 at r = 0), the xi shells' cell counts
+    (inf for an empty shell, as the reference), and the bispectrum of ``bispec``; the contrast is
+    transformed once per estimator on the device.
+    """
+    d = _cubic_mesh(delta)
+    k3d, pk, nm = powspec_vec(d, box_size, k_edges)
+    r3d, xi, nmx = _xi(d, _box_f32(box_size), s_edges, nan_mu_at_origin=False)
+    k_all, pkb, th, bk, qk = bispec(d, box_size, k1, k2, theta)
+    return k3d, pk, nm, r3d, xi, nmx, k_all, pkb, th, bk, qk

@@ -339,3 +339,13 @@ def bispec(delta, box_size, k1, k2, theta):
             qk[j] = bv / (pk[0] * pk[1] + pk[0] * pv + pk[1] * pv)
             pk[j + 2], bk[j] = pv, bv
     return k_all, pk, theta, bk, qk
+
+
+def compute_all_correlations(delta, box_size, s_edges, k_edges, k1, k2, theta):
+    """src/correlations.py:464-637: P_l(k) and xi_l(r) as compute_2pt_correlations (mu = 0 at the
+    origin, the real part of |delta_k|^2 transformed), the xi shells' cell counts (inf when empty), then
+    the bispectrum of bispec.  Returns (k3D, Pk3D, Nmodes3D_pk, r3D, xi3D, Nmodes3D_xi, k_all, Pk, theta, B, Q)."""
+    k3d, pk, nm = powspec_vec(delta, box_size, k_edges)
+    r3d, xi, nmx = _xi_core(delta, box_size, s_edges, mu_zero_at_origin=True)
+    k_all, pkb, th, bk, qk = bispec(delta, box_size, k1, k2, theta)
+    return k3d, pk, nm, r3d, xi, nmx, k_all, pkb, th, bk, qk

@@ -159,6 +159,19 @@ def main(root: str) -> None:
         out[f"bk_{i}_q"] = np.asarray(qk, F32)
     out["bk_ncases"] = np.array([len(bcases)])
 
+    # ---- compute_all_correlations (src/correlations.py:464-637) on the bispectrum cases' contrasts
+    for i, (N, box, k1, k2, nt) in enumerate(bcases):
+        delta, theta = out[f"bk_{i}_delta"], out[f"bk_{i}_theta"]
+        kf = 2 * np.pi / box
+        k_edges = np.arange(kf, np.pi * N / box, kf).astype(F32)
+        s_edges = np.linspace(0.0, 0.5 * box, 9).astype(F32)
+        res = corr.compute_all_correlations(delta, box, s_edges, k_edges, k1, k2, theta)
+        out[f"all_{i}_kedges"] = k_edges
+        out[f"all_{i}_sedges"] = s_edges
+        for name, v in zip(("k", "pk", "nmk", "r", "xi", "nmx", "kall", "pkb", "theta", "b", "q"), res):
+            out[f"all_{i}_{name}"] = np.asarray(v, F32)
+    out["all_ncases"] = np.array([len(bcases)])
+
     path = os.path.join(HERE, "reference_outputs.npz")
     np.savez_compressed(path, **out)
     print(f"wrote {path} ({os.path.getsize(path) / 1024:.0f} KiB, {len(out)} arrays)")

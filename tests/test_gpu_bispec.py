@@ -59,3 +59,28 @@ def test_bispectrum_is_deterministic():
     # k3 up to 0.3 h/Mpc reaches past the 128^3 grid's corner: those shells are empty, P = 0/0 (as the reference)
     pk, nm = a[1].cpu().numpy(), a[4].cpu().numpy()
     assert np.array_equal(np.isnan(pk), nm == 0) and (nm == 0).any() and (nm > 0).any()
+
+
+def test_compute_all_correlations_matches_reference(golden):
+    """Drop-in compute_all_correlations vs the fixtures of src/correlations.py:464-637."""
+    from gbpowspec import compute_all_correlations
+    for i in range(int(golden["all_ncases"][0])):
+        box, k1, k2 = golden[f"bk_{i}_args"]
+        g = lambda name: golden[f"all_{i}_{name}"]
+        k, pk, nmk, r, xi, nmx, kall, pkb, th, bk, qk = (
+            t.cpu().numpy() for t in compute_all_correlations(golden[f"bk_{i}_delta"], box, g("sedges"), g("kedges"),
+                                                              k1, k2, golden[f"bk_{i}_theta"]))
+        np.testing.assert_array_equal(k, g("k"))
+        np.testing.assert_array_equal(nmk, g("nmk"))
+        np.testing.assert_array_equal(r, g("r"))
+        np.testing.assert_array_equal(nmx, g("nmx"))
+        np.testing.assert_array_equal(th, g("theta"))
+        np.testing.assert_allclose(kall, g("kall"), rtol=2e-7)
+        assert np.array_equal(np.isnan(pk), np.isnan(g("pk"))) and np.array_equal(np.isnan(xi), np.isnan(g("xi")))
+        scale = np.abs(g("pk")[:, :1]) + 1e-30
+        assert np.nanmax(np.abs(pk - g("pk")) / scale) < 1e-5
+        # the first shell holds r = 0 (mu = 0 there), whose variance dominates its xi_2, xi_4: scale by all l
+        assert np.nanmax(np.abs(xi - g("xi"))) <= 1e-5 * np.nanmax(np.abs(g("xi")))
+        _assert_close(pkb, g("pkb"), 1e-5, "P")
+        _assert_close(bk, g("b"), 1e-5, "B")
+        _assert_close(qk, g("q"), 1e-5, "Q")

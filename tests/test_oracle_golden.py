@@ -161,3 +161,14 @@ def test_bispec_shell_decomposition():
         assert np.all(np.diff(edges) > 0) and edges[-1] > max(kmax.max(), kmin.max())
         np.testing.assert_array_equal(edges[sb[:, 0]], kmin)
         np.testing.assert_array_equal(edges[sb[:, 1]], kmax)
+
+
+def test_compute_all_correlations_restatement_bitexact(golden):
+    """oracle/reference_f32.compute_all_correlations reproduces src/correlations.py:464-637."""
+    names = ("k", "pk", "nmk", "r", "xi", "nmx", "kall", "pkb", "theta", "b", "q")
+    for i in range(int(golden["all_ncases"][0])):
+        box, k1, k2 = golden[f"bk_{i}_args"]
+        res = R.compute_all_correlations(golden[f"bk_{i}_delta"], box, golden[f"all_{i}_sedges"],
+                                         golden[f"all_{i}_kedges"], k1, k2, golden[f"bk_{i}_theta"])
+        for name, v in zip(names, res):
+            np.testing.assert_array_equal(np.asarray(v, np.float32), golden[f"all_{i}_{name}"], err_msg=name)
