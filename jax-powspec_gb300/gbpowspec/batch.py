@@ -118,6 +118,16 @@ class ParticleArena:
         self.dev.copy_(self.host, non_blocking=True)
         return self.nbytes
 
+    def upload_range(self, first: int, last: int) -> int:
+        """Enqueue the host-to-device copy of mocks first .. last-1 on the current stream (one copy per
+        particle column: the mocks are packed back to back); returns the bytes copied."""
+        if self.host is None:
+            raise RuntimeError("this arena lives on the device only")
+        a, b = int(self.offsets[first]), int(self.offsets[last])
+        for k in range(self.dev.shape[0]):
+            self.dev[k, a:b].copy_(self.host[k, a:b], non_blocking=True)
+        return (b - a) * 4 * self.dev.shape[0]
+
     def job_table(self, boxes, n_mesh: int, indices=None, origins=None) -> torch.Tensor:
         """Device table of gbp_job for mocks `indices` (default all) on an n_mesh grid.
 
@@ -234,6 +244,48 @@ class BatchRunner:
         o = self._out(res)
         check(_lib.load().gbp_batch_run(C.cast(self._lane_arr, C.c_void_p), lanes, C.c_void_p(jobs.data_ptr()), n,
                                         C.byref(o), _native._stream_of(self.device)), "gbp_batch_run")
+        return res
+
+    def _run_rows(self, jobs: torch.Tensor, first: int, last: int, res: BatchResult, lanes: int):
+        """gbp_batch_run over job rows first .. last-1, results into the same rows of `res`."""
+        nb = self.nb
+        o = _lib.LaneOut(res.pk.data_ptr() + first * nb * 3 * 8,
+                         None if res.kmean is None else res.kmean.data_ptr() + first * nb * 8,
+                         res.nmodes.data_ptr() + first * nb * 8, res.stats.data_ptr() + first * _lib.STATS_BYTES)
+        check(_lib.load().gbp_batch_run(C.cast(self._lane_arr, C.c_void_p), lanes,
+                                        C.c_void_p(jobs.data_ptr() + first * _lib.JOB_BYTES), last - first,
+                                        C.byref(o), _native._stream_of(self.device)), "gbp_batch_run")
+
+    def run_from_host(self, arena: "ParticleArena", jobs: torch.Tensor, out: BatchResult | None = None,
+                      chunk: int | None = None) -> BatchResult:
+        """Upload the arena's catalogues and process them, the copies overlapping the work: chunk c of
+        mocks is copied on a copy stream while the lanes process chunk c - 1 (default chunk: the lane
+        count).  Job row j must describe arena mock j (ParticleArena.job_table with the default indices).
+        Same results as ``arena.upload(); run(jobs)``; no host sync."""
+        n = int(jobs.shape[0])
+        if n != len(arena):
+            raise ValueError("run_from_host needs one job row per arena mock, in arena order")
+        if jobs.dtype != torch.uint8 or jobs.device != self.device or tuple(jobs.shape[1:]) != (_lib.JOB_BYTES,):
+            raise ValueError("jobs must be a device uint8 tensor [B, sizeof(gbp_job)] (ParticleArena.job_table)")
+        res = self.alloc_result(n) if out is None else out
+        if res.pk.shape[0] < n:
+            raise ValueError("result arrays hold fewer jobs than the table")
+        step = max(1, self.n_lanes if chunk is None else int(chunk))
+        cur = torch.cuda.current_stream(self.device)
+        if getattr(self, "_copy_stream", None) is None:
+            self._copy_stream = torch.cuda.Stream(self.device)
+        copy = self._copy_stream
+        copy.wait_stream(cur)            # earlier work that reads the arena's device buffer comes first
+        ready = []
+        with torch.cuda.stream(copy):
+            for a in range(0, n, step):
+                arena.upload_range(a, min(n, a + step))
+                ev = torch.cuda.Event()
+                ev.record(copy)
+                ready.append(ev)
+        for ev, a in zip(ready, range(0, n, step)):
+            cur.wait_event(ev)
+            self._run_rows(jobs, a, min(n, a + step), res, self.n_lanes)
         return res
 
     def run_one(self, jobs: torch.Tensor, index: int, out: BatchResult, lane: int = 0) -> BatchResult:

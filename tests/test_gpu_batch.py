@@ -145,3 +145,23 @@ def test_tune_lanes_returns_a_candidate():
     arena.upload()
     best, rates = tune_lanes(64, arena.job_table(500.0, 64), capacity=30_000, candidates=(1, 2), repeats=1)
     assert best in (1, 2) and set(rates) == {1, 2} and all(v > 0 for v in rates.values())
+
+
+def test_run_from_host_matches_upload_then_run():
+    """Chunked uploads overlapping the lanes give the same bits as one upload before the batch."""
+    from gbpowspec.batch import BatchRunner, ParticleArena
+    N, box = 64, 600.0
+    sizes = [30_000, 12_000, 45_000, 8_000, 27_000, 39_000, 16_000]
+    cats = _cats(sizes, box, seed0=700)
+    arena = ParticleArena(cats)
+    jobs = arena.job_table(box, N)
+    runner = BatchRunner(N, capacity=45_000, mas="tsc", interlace=True, ells=(0, 2, 4), n_lanes=3)
+    arena.upload()
+    want = runner.run(jobs)
+    torch.cuda.synchronize()
+    arena.dev.zero_()
+    for chunk in (None, 1, 2, 5):
+        got = runner.run_from_host(arena, jobs, chunk=chunk)
+        torch.cuda.synchronize()
+        assert _same(got.pk, want.pk) and torch.equal(got.nmodes, want.nmodes) and torch.equal(got.stats, want.stats)
+    runner.close()
