@@ -7,6 +7,7 @@
 #include <string.h>
 
 #include <map>
+#include <memory>
 #include <mutex>
 #include <new>
 #include <tuple>
@@ -23,31 +24,60 @@ static thread_local int g_last_cufft = 0;
 void set_last_cuda_error(cudaError_t e) { g_last_cuda = e; }
 void set_last_cufft_error(int code) { g_last_cufft = code; }
 
-int c2r_plan(int N, int P, int batch, cufftHandle* out, size_t* ws) {
+namespace {
+struct C2RPlan {
+  cufftHandle h;
+  size_t ws;
+  std::mutex use;      // held while a call sets the stream and work area and enqueues the transform
+};
+
+int c2r_entry(int N, int P, int batch, C2RPlan** out) {
   static std::mutex mu;
-  static std::map<std::tuple<int, int, int, int>, std::pair<cufftHandle, size_t>> cache;
+  static std::map<std::tuple<int, int, int, int>, std::unique_ptr<C2RPlan>> cache;
   int dev = 0;
   cudaGetDevice(&dev);
   const auto key = std::make_tuple(dev, N, P, batch);
   std::lock_guard<std::mutex> lock(mu);
   auto it = cache.find(key);
   if (it == cache.end()) {
-    cufftHandle h;
-    GBP_CUFFT_TRY(cufftCreate(&h));
-    cufftSetAutoAllocation(h, 0);
+    std::unique_ptr<C2RPlan> e(new (std::nothrow) C2RPlan());
+    if (!e) return GBP_ERR_ALLOC;
+    GBP_CUFFT_TRY(cufftCreate(&e->h));
+    cufftSetAutoAllocation(e->h, 0);
     int n[3] = {N, N, N}, inembed[3] = {N, N, P}, onembed[3] = {N, N, N};
     size_t w = 0;
     const int mr =
-        (int)cufftMakePlanMany(h, 3, n, inembed, 1, N * N * P, onembed, 1, N * N * N, CUFFT_C2R, batch, &w);
+        (int)cufftMakePlanMany(e->h, 3, n, inembed, 1, N * N * P, onembed, 1, N * N * N, CUFFT_C2R, batch, &w);
     if (mr != 0) {
-      cufftDestroy(h);
+      cufftDestroy(e->h);
       set_last_cufft_error(mr);
       return GBP_ERR_CUFFT;
     }
-    it = cache.emplace(key, std::make_pair(h, w)).first;
+    e->ws = w;
+    it = cache.emplace(key, std::move(e)).first;
   }
-  *out = it->second.first;
-  *ws = it->second.second;
+  *out = it->second.get();
+  return GBP_OK;
+}
+}  // namespace
+
+int c2r_plan(int N, int P, int batch, cufftHandle* out, size_t* ws) {
+  C2RPlan* e = nullptr;
+  const int r = c2r_entry(N, P, batch, &e);
+  if (r) return r;
+  *out = e->h;
+  *ws = e->ws;
+  return GBP_OK;
+}
+
+int c2r_exec(int N, int P, int batch, const float2* in, float* out, void* work, cudaStream_t st) {
+  C2RPlan* e = nullptr;
+  const int r = c2r_entry(N, P, batch, &e);
+  if (r) return r;
+  std::lock_guard<std::mutex> lock(e->use);
+  GBP_CUFFT_TRY(cufftSetStream(e->h, st));
+  GBP_CUFFT_TRY(cufftSetWorkArea(e->h, work));
+  GBP_CUFFT_TRY(cufftExecC2R(e->h, reinterpret_cast<cufftComplex*>(const_cast<float2*>(in)), out));
   return GBP_OK;
 }
 

@@ -306,14 +306,9 @@ extern "C" int gbp_bispec(gbp_fft_plan plan, const float* delta, void* spectrum,
   }
   // 3. their fields
   {
-    cufftHandle h;
-    size_t w = 0;
-    r = c2r_plan(N, L.Pc, 4, &h, &w);
-    if (r) return r;
     GBP_TRACE("bispec_c2r", st);
-    GBP_CUFFT_TRY(cufftSetStream(h, st));
-    GBP_CUFFT_TRY(cufftSetWorkArea(h, cws));
-    GBP_CUFFT_TRY(cufftExecC2R(h, reinterpret_cast<cufftComplex*>(A), R));
+    r = c2r_exec(N, L.Pc, 4, A, R, cws, st);
+    if (r) return r;
   }
   // 4. delta_1 delta_2 and I_1 I_2
   int dev = 0, sms = 0;

@@ -33,6 +33,11 @@ int xbin_power_workspace(gbp_fft_plan plan, gbp_bins bins, int ells, size_t* byt
 // real output [batch][N][N][N].  No work area of its own: *ws bytes are
 // passed with cufftSetWorkArea (0 when the plan needs none).
 int c2r_plan(int N, int P, int batch, cufftHandle* h, size_t* ws);
+// Enqueue that transform on `st` with `work` (>= ws bytes, its own region:
+// not the input) as the work area; the plan's stream and work area are set
+// and the transform enqueued under a lock, so concurrent callers cannot mix
+// them up.  `in` is overwritten (cuFFT's multi-dimensional C2R).
+int c2r_exec(int N, int P, int batch, const float2* in, float* out, void* work, cudaStream_t st);
 int xbin_power(gbp_fft_plan plan, float2* spec, gbp_bins bins, int mas_order, int ells, const double* mass,
                double* sums_out, long long* nmodes_out, double* ksum_out, void* ws, size_t ws_bytes,
                cudaStream_t st);

@@ -217,11 +217,10 @@ extern "C" int gbp_power_backward(const void* spectrum, gbp_fft_plan plan, gbp_b
     GBP_LAUNCH_CHECK();
   }
   GBP_TRACE("grad_c2r", st);
-  GBP_CUFFT_TRY(cufftSetStream(h, st));
-  GBP_CUFFT_TRY(cufftSetWorkArea(h, cws));
-  for (int g = 0; g < G; ++g)
-    GBP_CUFFT_TRY(cufftExecC2R(h, reinterpret_cast<cufftComplex*>(hspec + g * total),
-                               grad_mesh + (long long)g * N * N * N));
+  for (int g = 0; g < G; ++g) {
+    r = c2r_exec(N, P, 1, hspec + g * total, grad_mesh + (long long)g * N * N * N, cws, st);
+    if (r) return r;
+  }
   return GBP_OK;
 }
 

@@ -190,15 +190,10 @@ extern "C" int gbp_xi(gbp_fft_plan plan, const float* delta, void* spectrum, flo
     GBP_LAUNCH_CHECK();
   }
   // 3. inverse real transform (unnormalised)
-  cufftHandle h;
-  size_t w = 0;
-  r = c2r_plan(N, P, 1, &h, &w);
-  if (r) return r;
   {
     GBP_TRACE("xi_c2r", st);
-    if (cufftSetStream(h, st) != CUFFT_SUCCESS || cufftSetWorkArea(h, cws) != CUFFT_SUCCESS ||
-        cufftExecC2R(h, reinterpret_cast<cufftComplex*>(spec), field) != CUFFT_SUCCESS)
-      return GBP_ERR_CUFFT;
+    r = c2r_exec(N, P, 1, spec, field, cws, st);
+    if (r) return r;
   }
   // 4. separation shells
   PowGeom g{};

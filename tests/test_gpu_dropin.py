@@ -171,3 +171,30 @@ def test_xi_of_a_large_mesh_against_fp64():
     want = want / cnt[:, None] / N ** 3
     np.testing.assert_array_equal(nm.cpu().numpy(), cnt.astype(np.float32))
     _assert_xi(xi.cpu().numpy(), want, None)
+
+
+def test_xi_from_concurrent_threads_matches_serial():
+    """Two host threads on their own streams share the cached inverse-transform plan: same bits as one at a time."""
+    import threading
+    from gbpowspec import xi_vec
+    rng = np.random.default_rng(11)
+    deltas = [torch.from_numpy(rng.standard_normal((64, 64, 64)).astype(np.float32)).cuda() for _ in range(2)]
+    se = np.arange(2.0, 60.0, 4.0).astype(np.float32)
+    want = [xi_vec(d, 500.0, se)[1].cpu() for d in deltas]
+    got = [None, None]
+
+    def work(i):
+        s = torch.cuda.Stream()
+        with torch.cuda.stream(s):
+            for _ in range(20):
+                r = xi_vec(deltas[i], 500.0, se)[1]
+            s.synchronize()
+            got[i] = r.cpu()
+
+    ts = [threading.Thread(target=work, args=(i,)) for i in range(2)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    for a, b in zip(got, want):
+        assert np.array_equal(a.numpy(), b.numpy(), equal_nan=True)
