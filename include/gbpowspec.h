@@ -88,7 +88,10 @@ typedef struct gbp_deposit_stats {
   double sum_w2;        /* sum of squared weights (shot noise)              */
   long long n_kept;     /* particles that deposited at least one cell       */
   long long n_nonfinite;/* particles dropped for a non-finite coordinate    */
-  int scale_exp;        /* fixed-point exponent s used by the accumulation  */
+  int scale_exp;        /* fixed-point exponent s of the mass totals (the
+                           mesh deposit accumulates at 2^s; the fused deposit
+                           of gbp_particles_power at 2^(s - t) per tile, t >= 0
+                           from the tile's occupancy, its totals shifted to 2^s) */
   int pad_;
 } gbp_deposit_stats;
 
@@ -272,8 +275,10 @@ int gbp_fft_power(gbp_fft_plan plan, const float* mesh, void* spectrum,
  * of the FFT (library transform sizes: power-of-two meshes 64..1024 and a
  * plan made without the cuFFT override; B-spline deposits).  The mesh is
  * never written: each column tile of pencils is deposited in shared memory
- * and transformed along z there; then the y pass and the x pass fused with
- * the binning.  Interlacing follows the plan (2 grids = interlaced).
+ * (32-bit fixed point at a scale per tile that no cell can overflow, exact
+ * and order-independent) and transformed along z there; then the y pass and
+ * the x pass fused with the binning.  Interlacing follows the plan (2 grids
+ * = interlaced).
  * Outputs as gbp_deposit (stats_out, required: it carries the mass the
  * binning and the normalisation use) followed by gbp_fft_power; `spectrum`
  * is scratch of the plan's spectrum size.  Replaces src/mas.py:88-153 +
