@@ -522,7 +522,9 @@ def main():
                 "d2h_bytes_per_step": int(pk_host.numel() * 8),
                 "path": "BatchRunner.run_from_host (pinned H2D of every mock, chunk by chunk on a copy stream "
                         "overlapping the lanes) + P_l D2H"},
-        "gpu_launches": int(round(per_mock_launches)) * args.steps * B + lanes * args.steps,
+        # per mock: the traced stages (the scan stage is two cub kernels) + lane_begin + lane_end; per batch
+        # call: one descriptor kernel per lane
+        "gpu_launches": int(round(per_mock_launches + 1 + 2)) * args.steps * B + lanes * args.steps,
         "clocks": clk,
         **extra,
     }
