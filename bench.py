@@ -307,8 +307,9 @@ def serving_leg(dev, seed: int, seconds: float = 1.0, rate: float = 200.0) -> di
 
 
 def extensions_leg(dev, seed: int, reps: int = 5) -> dict:
-    """Milliseconds per call (median of `reps` after a warm call, CUDA events) of the estimators beside
-    P_l(k): xi_l(r) of a 256^3 contrast (xi_vec), the bispectrum of a 256^3 contrast at k1 = 0.1, k2 = 0.2,
+    """Milliseconds per call (median of `reps` after a warm call, CUDA events) of the reference's own call
+    sequence through the drop-ins (cic_mas_vec -> delta/mean - 1 -> powspec_vec on the headline mock) and
+    of the estimators beside P_l(k): xi_l(r) of a 256^3 contrast (xi_vec), the bispectrum of a 256^3 contrast at k1 = 0.1, k2 = 0.2,
     20 angles in [0, pi], L = 2500 (bispec; the reference's tests/bispec.py case), and P_l(k) forward +
     backward (gradients for 1,048,576 particle positions and weights, 256^3 TSC + interlacing)."""
     import torch
@@ -341,7 +342,26 @@ def extensions_leg(dev, seed: int, reps: int = 5) -> dict:
         pk = power_multipoles_diff(*pos, box_size=box, n_mesh=256, mas="tsc", interlace=True)
         torch.nan_to_num(pk, nan=0.0).sum().backward()
 
-    return {"xi_vec_256_ms": med_ms(lambda: xi_vec(d, box, s_edges)),
+    # the reference's own call sequence through the drop-ins on the headline mock (512^3, 4,194,304
+    # particles): cic_mas_vec (its CIC, corner weight and all) -> delta / mean - 1 -> powspec_vec
+    from gbpowspec import cic_mas_vec, powspec_vec
+    xh, yh, zh = make_catalogue(seed=seed)
+    xd_, yd_, zd_ = (torch.from_numpy(a).to(dev) for a in (xh, yh, zh))
+    wd_ = torch.ones_like(xd_)
+    N512, L = 512, float(CONFIG["box"])
+    mesh0 = torch.zeros((N512, N512, N512), dtype=torch.float32, device=dev)
+    kf = 2.0 * np.pi / L
+    k_edges = np.arange(kf, np.pi * N512 / L, kf).astype(np.float32)
+
+    def dropin():
+        m = cic_mas_vec(mesh0, xd_, yd_, zd_, wd_, xd_.numel(), 0.0, 0.0, 0.0, L, N512, True)
+        m = m / m.mean() - 1.0
+        return powspec_vec(m, L, k_edges)
+
+    t_dropin = med_ms(dropin)
+    del mesh0
+    return {"dropin_cic_mas_vec_powspec_vec_512_ms": t_dropin,
+            "xi_vec_256_ms": med_ms(lambda: xi_vec(d, box, s_edges)),
             "bispec_256_20_angles_ms": med_ms(lambda: bispectrum(d, box, 0.1, 0.2, theta)),
             "power_grad_256_tsc_interlaced_1M_particles_ms": med_ms(grad_step)}
 
