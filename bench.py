@@ -360,7 +360,23 @@ def extensions_leg(dev, seed: int, reps: int = 5) -> dict:
 
     t_dropin = med_ms(dropin)
     del mesh0
+    # the reference's CPU-runnable case: 1,048,576 uniform particles, L = 1000, 128^3 CIC, monopole, k bins
+    # of width kF from kF to k_Nyq, through the same drop-in sequence
+    g1 = torch.Generator(device=dev).manual_seed(seed)
+    u1 = [torch.rand(1 << 20, generator=g1, device=dev) * 1000.0 for _ in range(3)]
+    w1 = torch.ones_like(u1[0])
+    mesh1 = torch.zeros((128, 128, 128), dtype=torch.float32, device=dev)
+    kf1 = 2.0 * np.pi / 1000.0
+    edges1 = np.arange(kf1, np.pi * 128 / 1000.0, kf1).astype(np.float32)
+
+    def config1():
+        m = cic_mas_vec(mesh1, *u1, w1, u1[0].numel(), 0.0, 0.0, 0.0, 1000.0, 128, True)
+        m = m / m.mean() - 1.0
+        return powspec_vec(m, 1000.0, edges1)
+
+    t_config1 = med_ms(config1)
     return {"dropin_cic_mas_vec_powspec_vec_512_ms": t_dropin,
+            "config1_uniform_1M_128_cic_dropin_ms": t_config1,
             "xi_vec_256_ms": med_ms(lambda: xi_vec(d, box, s_edges)),
             "bispec_256_20_angles_ms": med_ms(lambda: bispectrum(d, box, 0.1, 0.2, theta)),
             "power_grad_256_tsc_interlaced_1M_particles_ms": med_ms(grad_step)}
