@@ -7,15 +7,17 @@ import torch
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("mas,interlace,weights", [("cic", False, True), ("tsc", True, True), ("pcs", True, False),
-                                                   ("tsc", False, False)])
-def test_gradients_match_fp64_autograd(mas, interlace, weights):
+@pytest.mark.parametrize("mas,interlace,weights,N", [("cic", False, True, 32), ("tsc", True, True, 32),
+                                                     ("pcs", True, False, 32), ("tsc", False, False, 32),
+                                                     ("tsc", True, True, 64), ("cic", False, False, 64)])
+def test_gradients_match_fp64_autograd(mas, interlace, weights, N):
+    """N = 32: cuFFT spectra (rows of N/2+1); N = 64: the library transform's (rows of N/2+8)."""
     import fp64_torch as F
     from gbpowspec.grad import power_multipoles_diff
     from gbpowspec.pipeline import PkConfig
     from gbpowspec.synth import lognormal_catalogue
     from gbpowspec._lib import MAS
-    N, box, n = 32, 400.0, 3000
+    box, n = 400.0, 3000
     x, y, z = lognormal_catalogue(n, box, grid=32, seed=5)
     rng = np.random.default_rng(6)
     w = rng.uniform(0.5, 1.5, n).astype(np.float32) if weights else None
