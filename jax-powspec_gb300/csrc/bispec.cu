@@ -167,23 +167,15 @@ bispec_bin_kernel(PowGeom g, const float2* __restrict__ sD, const float2* __rest
   }
 }
 
-// One warp per elementary bin: the C group partials in a fixed order, in double.
-__global__ void bispec_reduce_kernel(const float2* __restrict__ part_ff, int C, int nbe, double* E) {
-  const int b = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
-  if (b >= nbe) return;
-  for (int q = 0; q < BK_NV; ++q) {
-    ff acc{0.f, 0.f};
-    for (int c = lane; c < C; c += 32) {
-      const float2 v = part_ff[((long long)c * BK_NV + q) * nbe + b];
-      acc = ff_add(acc, ff{v.x, v.y});
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-      ff t{__shfl_xor_sync(0xffffffffu, acc.hi, o), __shfl_xor_sync(0xffffffffu, acc.lo, o)};
-      acc = ff_add(acc, t);
-    }
-    if (lane == 0) E[b * BK_NV + q] = (double)acc.hi + (double)acc.lo;
-  }
+// One block per elementary bin: the C group partials folded in a fixed order (fold_bin).
+__global__ void __launch_bounds__(FOLD_THREADS)
+bispec_reduce_kernel(const float2* __restrict__ part_ff, int C, int nbe, double* E) {
+  const int b = blockIdx.x;
+  if (b >= nbe) return;                        // uniform over the block
+  double m[BK_NV] = {0.0, 0.0, 0.0, 0.0};
+  fold_bin<BK_NV>(part_ff, C, BK_NV, nbe, b, m);
+  if (threadIdx.x == 0)
+    for (int q = 0; q < BK_NV; ++q) E[b * BK_NV + q] = m[q];
 }
 
 struct ShellSums {
@@ -360,8 +352,7 @@ extern "C" int gbp_bispec(gbp_fft_plan plan, const float* delta, void* spectrum,
   }
   {
     GBP_TRACE("bispec_reduce", st);
-    const int wpb = 8;
-    bispec_reduce_kernel<<<(B->nbe + wpb - 1) / wpb, wpb * 32, 0, st>>>(part, L.C, B->nbe, E);
+    bispec_reduce_kernel<<<B->nbe, FOLD_THREADS, 0, st>>>(part, L.C, B->nbe, E);
     GBP_LAUNCH_CHECK();
   }
   {

@@ -367,9 +367,8 @@ extern "C" int gbp_power(const void* spectrum, int G, int z_pitch, gbp_bins B, i
     kern<<<grid, L.warps * 32, L.smem, stream>>>(g);
     GBP_LAUNCH_CHECK();
   }
-  const int wpb = 8;
   GBP_TRACE("power_reduce", stream);
-  power_reduce_kernel<<<(B->nb + wpb - 1) / wpb, wpb * 32, 0, stream>>>(
+  power_reduce_kernel<<<B->nb, FOLD_THREADS, 0, stream>>>(
       part_ff, L.C, L.NV, B->nb, B->nbe, B->d_nmodes, B->d_ksum, sums_out, nmodes_out,
       (ells & GBP_KSUM) ? ksum_out : nullptr);
   GBP_LAUNCH_CHECK();
@@ -519,9 +518,8 @@ extern "C" int gbp_power_noalloc(const void* spectrum, int G, int z_pitch, gbp_b
     kern<<<grid, L.warps * 32, L.smem, stream>>>(g);
     GBP_LAUNCH_CHECK();
   }
-  const int wpb = 8;
   GBP_TRACE("power_reduce", stream);
-  power_reduce_kernel<<<(B->nb + wpb - 1) / wpb, wpb * 32, 0, stream>>>(
+  power_reduce_kernel<<<B->nb, FOLD_THREADS, 0, stream>>>(
       part_ff, L.C, L.NV, B->nb, B->nbe, B->d_nmodes, B->d_ksum, sums_out, nmodes_out,
       (ells & GBP_KSUM) ? ksum_out : nullptr);
   GBP_LAUNCH_CHECK();

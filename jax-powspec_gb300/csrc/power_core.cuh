@@ -189,30 +189,51 @@ __device__ __forceinline__ void cta_fold(const PowGeom& g, const Smem& s, int gr
   __syncthreads();
 }
 
-// One warp per bin: fold the CTA partials (fixed order) into double moment
-// totals and form the Legendre sums; copy the plan's geometry per bin.
-__global__ void power_reduce_kernel(const float2* __restrict__ part_ff, int C, int NV, int nb, int nbe,
-                                    const long long* __restrict__ plan_nmodes, const double* __restrict__ plan_ksum,
-                                    double* sums_out, long long* nmodes_out, double* ksum_out) {
-  const int b = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
-  if (b >= nb) return;
-  double m[3] = {0.0, 0.0, 0.0};
-  if (b < nbe) {
+// Fold of one bin's group partials (float-float, [C][NV][nbe] layout) into
+// doubles, by a whole block of FOLD_THREADS: thread t takes groups t, t +
+// FOLD_THREADS, ...; each warp folds its lanes by a fixed xor tree; thread 0
+// folds the warps in order.  Fixed order throughout: bitwise reproducible.
+// Only thread 0 receives the results; every thread of the block must call.
+constexpr int FOLD_THREADS = 256;
+
+template <int MAXV>
+__device__ __forceinline__ void fold_bin(const float2* __restrict__ part_ff, int C, int NV, int nbe, int b,
+                                         double (&m)[MAXV]) {
+  __shared__ ff s_w[MAXV][FOLD_THREADS / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int q = 0; q < NV; ++q) {
+    ff acc{0.f, 0.f};
+    for (int c = threadIdx.x; c < C; c += FOLD_THREADS) {
+      const float2 v = part_ff[((long long)c * NV + q) * nbe + b];
+      acc = ff_add(acc, ff{v.x, v.y});
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      ff t{__shfl_xor_sync(0xffffffffu, acc.hi, o), __shfl_xor_sync(0xffffffffu, acc.lo, o)};
+      acc = ff_add(acc, t);
+    }
+    if (lane == 0) s_w[q][warp] = acc;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
     for (int q = 0; q < NV; ++q) {
-      ff acc{0.f, 0.f};
-      for (int c = lane; c < C; c += 32) {
-        const float2 v = part_ff[((long long)c * NV + q) * nbe + b];
-        acc = ff_add(acc, ff{v.x, v.y});
-      }
-      for (int o = 16; o > 0; o >>= 1) {
-        ff t{__shfl_xor_sync(0xffffffffu, acc.hi, o), __shfl_xor_sync(0xffffffffu, acc.lo, o)};
-        acc = ff_add(acc, t);
-      }
-      m[q] = (double)acc.hi + (double)acc.lo;
+      ff t = s_w[q][0];
+      for (int w = 1; w < FOLD_THREADS / 32; ++w) t = ff_add(t, s_w[q][w]);
+      m[q] = (double)t.hi + (double)t.lo;
     }
   }
-  if (lane == 0) {
+}
+
+// One block per bin (FOLD_THREADS threads): fold the CTA partials into double
+// moment totals and form the Legendre sums; copy the plan's geometry per bin.
+__global__ void __launch_bounds__(FOLD_THREADS)
+power_reduce_kernel(const float2* __restrict__ part_ff, int C, int NV, int nb, int nbe,
+                    const long long* __restrict__ plan_nmodes, const double* __restrict__ plan_ksum,
+                    double* sums_out, long long* nmodes_out, double* ksum_out) {
+  const int b = blockIdx.x;
+  if (b >= nb) return;                         // uniform over the block
+  double m[3] = {0.0, 0.0, 0.0};
+  if (b < nbe) fold_bin<3>(part_ff, C, NV, nbe, b, m);
+  if (threadIdx.x == 0) {
     sums_out[b * 3 + 0] = m[0];
     sums_out[b * 3 + 1] = NV > 1 ? 1.5 * m[1] - 0.5 * m[0] : 0.0;
     sums_out[b * 3 + 2] = NV > 2 ? (35.0 * m[2] - 30.0 * m[1] + 3.0 * m[0]) * 0.125 : 0.0;

@@ -353,9 +353,8 @@ int xbin_power(gbp_fft_plan plan, float2* spec, gbp_bins B, int mas_order, int e
     default: r = GBP_ERR_UNSUPPORTED;
   }
   if (r) return r;
-  const int wpb = 8;
   GBP_TRACE("power_reduce", st);
-  power_reduce_kernel<<<(B->nb + wpb - 1) / wpb, wpb * 32, 0, st>>>(
+  power_reduce_kernel<<<B->nb, FOLD_THREADS, 0, st>>>(
       g.part_ff, L.groups, L.NV, B->nb, B->nbe, B->d_nmodes, B->d_ksum, sums_out, nmodes_out,
       (ells & GBP_KSUM) ? ksum_out : nullptr);
   GBP_LAUNCH_CHECK();

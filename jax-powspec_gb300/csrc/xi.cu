@@ -94,27 +94,16 @@ xi_bin_kernel(PowGeom g, const float* __restrict__ field, int nan_origin) {
   }
 }
 
-__global__ void xi_reduce_kernel(const float2* __restrict__ part_ff, int C, int nb, int nbe, double* sums_out,
-                                 long long* counts_out) {
-  const int b = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
-  if (b >= nb) return;
+// One block per bin: the group partials folded in a fixed order (fold_bin),
+// then the Legendre sums and the cell count.
+__global__ void __launch_bounds__(FOLD_THREADS)
+xi_reduce_kernel(const float2* __restrict__ part_ff, int C, int nb, int nbe, double* sums_out,
+                 long long* counts_out) {
+  const int b = blockIdx.x;
+  if (b >= nb) return;                         // uniform over the block
   double m[XI_NV] = {0.0, 0.0, 0.0, 0.0};
-  if (b < nbe) {
-    for (int q = 0; q < XI_NV; ++q) {
-      ff acc{0.f, 0.f};
-      for (int c = lane; c < C; c += 32) {
-        const float2 v = part_ff[((long long)c * XI_NV + q) * nbe + b];
-        acc = ff_add(acc, ff{v.x, v.y});
-      }
-      for (int o = 16; o > 0; o >>= 1) {
-        ff t{__shfl_xor_sync(0xffffffffu, acc.hi, o), __shfl_xor_sync(0xffffffffu, acc.lo, o)};
-        acc = ff_add(acc, t);
-      }
-      m[q] = (double)acc.hi + (double)acc.lo;
-    }
-  }
-  if (lane == 0) {
+  if (b < nbe) fold_bin<XI_NV>(part_ff, C, XI_NV, nbe, b, m);
+  if (threadIdx.x == 0) {
     sums_out[b * 3 + 0] = m[0];
     sums_out[b * 3 + 1] = 1.5 * m[1] - 0.5 * m[0];
     sums_out[b * 3 + 2] = (35.0 * m[2] - 30.0 * m[1] + 3.0 * m[0]) * 0.125;
@@ -226,8 +215,7 @@ extern "C" int gbp_xi(gbp_fft_plan plan, const float* delta, void* spectrum, flo
   }
   {
     GBP_TRACE("xi_reduce", st);
-    const int wpb = 8;
-    xi_reduce_kernel<<<(B->nb + wpb - 1) / wpb, wpb * 32, 0, st>>>(part, L.C, B->nb, B->nbe, sums_out, counts_out);
+    xi_reduce_kernel<<<B->nb, FOLD_THREADS, 0, st>>>(part, L.C, B->nb, B->nbe, sums_out, counts_out);
     GBP_LAUNCH_CHECK();
   }
   return GBP_OK;
