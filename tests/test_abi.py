@@ -39,3 +39,30 @@ def test_status_strings_and_version():
 def test_library_path_is_in_tree():
     from gbpowspec import _lib
     assert os.path.commonpath([_lib.lib_path(), ROOT]) == ROOT
+
+
+def test_header_is_plain_c_and_links(tmp_path):
+    """A C client (cgo, a C program) can include the header as C99 and link the library."""
+    import shutil
+    import subprocess
+    if shutil.which("gcc") is None:
+        pytest.skip("no C compiler")
+    from gbpowspec import _lib
+    lib = _lib.lib_path()
+    _lib.load()                                  # builds the library when it is missing
+    src = tmp_path / "client.c"
+    src.write_text('#include "gbpowspec.h"\n'
+                   'int main(void) {\n'
+                   '  size_t b = 0;\n'
+                   '  int32_t thr[3], last = 0; int reach = 0;\n'
+                   '  const float e[3] = {1.0f, 2.0f, 3.0f};\n'
+                   '  if (gbp_version() < 100) return 1;\n'
+                   '  if (gbp_bin_thresholds(e, 3, 16, thr, &last, &reach) != GBP_OK) return 2;\n'
+                   '  (void)b;\n'
+                   '  return (thr[0] == 1 && thr[1] == 4 && thr[2] == 9) ? 0 : 3;\n'
+                   '}\n')
+    exe = tmp_path / "client"
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I",
+                    os.path.join(ROOT, "include"), str(src), "-o", str(exe), lib,
+                    "-Wl,-rpath," + os.path.dirname(lib)], check=True, capture_output=True)
+    assert subprocess.run([str(exe)]).returncode == 0
