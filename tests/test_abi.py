@@ -66,3 +66,23 @@ def test_header_is_plain_c_and_links(tmp_path):
                     os.path.join(ROOT, "include"), str(src), "-o", str(exe), lib,
                     "-Wl,-rpath," + os.path.dirname(lib)], check=True, capture_output=True)
     assert subprocess.run([str(exe)]).returncode == 0
+
+
+def test_entry_points_reject_bad_arguments_before_any_device_work():
+    """Null plans, buffers or negative sizes come back as GBP_ERR_INVALID on a host without a GPU."""
+    import ctypes as C
+    from gbpowspec import _lib
+    lib = _lib.load()
+    inv = _lib.GBP_ERR_INVALID
+    null = None
+    sz = C.c_size_t(0)
+    assert lib.gbp_xi_workspace_size(null, null, C.byref(sz)) == inv
+    assert lib.gbp_xi(null, null, null, null, null, 2, 1, null, null, null, 0, null) == inv
+    assert lib.gbp_bispec_workspace_size(null, null, C.byref(sz)) == inv
+    assert lib.gbp_bispec(null, null, null, null, 2, null, 3, 1000.0, null, null, null, null, null, 0, null) == inv
+    assert lib.gbp_power_backward_workspace_size(null, C.byref(sz)) == inv
+    assert lib.gbp_power_backward(null, null, null, 2, null, null, null, 1000.0, null, null, 0, null) == inv
+    assert lib.gbp_deposit_backward(null, null, null, null, -1, 0.0, 0.0, 0.0, 1.0, 64, 2, 0, null, null, null,
+                                    null, null, null) == inv
+    assert lib.gbp_deposit_backward(null, null, null, null, 10, 0.0, 0.0, 0.0, 1.0, 64, 9, 0, null, null, null,
+                                    null, null, null) == inv
