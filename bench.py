@@ -375,8 +375,19 @@ def extensions_leg(dev, seed: int, reps: int = 5) -> dict:
         return powspec_vec(m, 1000.0, edges1)
 
     t_config1 = med_ms(config1)
+    del mesh1, u1, w1
+    # config 3's mesh: 1024^3, 16,777,216 lognormal particles, PCS + interlacing, P_0,2,4 (production path)
+    from gbpowspec import PkConfig, PowerSpectrum
+    torch.cuda.empty_cache()
+    x3, y3, z3 = lognormal_catalogue_gpu(1 << 24, 2500.0, grid=256, seed=seed + 3, device=dev)
+    ps3 = PowerSpectrum(PkConfig(n_mesh=1024, box_size=2500.0, mas="pcs", interlace=True), dev)
+    ps3.reserve(x3.numel())
+    t_config3 = med_ms(lambda: ps3.run(x3, y3, z3))
+    del ps3, x3, y3, z3
+    torch.cuda.empty_cache()
     return {"dropin_cic_mas_vec_powspec_vec_512_ms": t_dropin,
             "config1_uniform_1M_128_cic_dropin_ms": t_config1,
+            "config3_1024_pcs_interlaced_16M_ms": t_config3,
             "xi_vec_256_ms": med_ms(lambda: xi_vec(d, box, s_edges)),
             "bispec_256_20_angles_ms": med_ms(lambda: bispectrum(d, box, 0.1, 0.2, theta)),
             "power_grad_256_tsc_interlaced_1M_particles_ms": med_ms(grad_step)}
