@@ -214,9 +214,9 @@ int gbp_power(const void* spectrum, int n_grids, int z_pitch, gbp_bins bins,
  * gbp_power without a workspace argument: the same result, with its scratch
  * held in a fixed 16 MiB device array inside the library, for callers that
  * cannot allocate device memory when they call in (a JAX/XLA custom call gets
- * only its operand and result buffers; a thread recording the stream into a
- * CUDA graph may not cudaMalloc).  This entry point has no counterpart in the
- * reference.
+ * only its operand and result buffers, and its device memory belongs to
+ * JAX's allocator, which reserves most of the GPU up front).  This entry
+ * point has no counterpart in the reference.
  * Limit: (work groups) x (moments) x (bins) <= 2^21 float2, which holds any
  * 512^3 mesh with up to ~560 bins of l = 0,2,4; larger requests return
  * GBP_ERR_UNSUPPORTED without launching.  The first call on a device looks up
@@ -316,6 +316,16 @@ int gbp_lognormal(int grid, double box, double k_cut, double sigma_v,
                   int64_t n, unsigned long long seed, float* x, float* y,
                   float* z, void* workspace, size_t workspace_bytes,
                   gbp_stream_t stream);
+/* The field behind gbp_lognormal's catalogue for the same (grid, box, k_cut,
+ * seed), on the grid^3 lattice (x slowest, z fastest): g_out the Gaussian
+ * field g (replaces src/gauss_field.py:5-80 gaussian_field, which returns the
+ * field of a tabulated P(k)), rho_out = exp(g - 1/2) = 1 + delta_LN, the
+ * density that gbp_lognormal samples its particles from.  Either pointer may
+ * be NULL, not both.  Same workspace as gbp_lognormal. */
+int gbp_lognormal_field(int grid, double box, double k_cut,
+                        unsigned long long seed, float* g_out, float* rho_out,
+                        void* workspace, size_t workspace_bytes,
+                        gbp_stream_t stream);
 /* Host evaluation of the generator's Philox4x32-10 block (known-answer
  * tests): out = philox(ctr[4], key[2]). */
 int gbp_philox4x32_10(const unsigned* ctr, const unsigned* key, unsigned* out);

@@ -29,6 +29,9 @@
 // finish the transform and the P_l sums.  HBM traffic per grid: the
 // spectrum is written once here, read and written by the y pass, and read
 // once by the binning; no mesh goes through HBM.
+#include <algorithm>
+#include <type_traits>
+
 #include "deposit_core.cuh"
 #include "fft_pass.cuh"
 #include "gbp_bins.h"
@@ -47,7 +50,135 @@ struct ColTile {
   static constexpr int NT = NFFT < 256 ? 256 : NFFT;
   static constexpr int MINB = NT >= 512 ? 2 : 3;  // CTAs per SM the registers are sized for
   static constexpr size_t SMEM = (size_t)(NPEN + 1) * N * sizeof(int);   // cells + per-plane entry counts
+  static constexpr size_t SMEM_WIDE = (size_t)NPEN * N * sizeof(long long);
 };
+
+// Bits of resolution a tile may give up to its 32-bit cells.  A tile whose
+// densest z plane is covered by more than 2^(SH_MAX + WBIT) entries (a dense
+// clump: a halo, a point mass) is deposited with 64-bit cells at the common
+// scale instead, by deposit_fftz_wide_kernel: with the coarse quantum the
+// rounding of many identical contributions adds up instead of averaging out.
+constexpr int SH_MAX = 10;
+constexpr long long WIDE_MARK = (-0x7fffffffffffffffLL - 1);   // tile_mass entry of a tile left to the wide kernel
+
+// Deposit, z transform, split and row stores of one column tile and grid
+// (steps 1-4 above).  WIDE: 64-bit cells at the common scale 2^sg (sh = 0);
+// otherwise 32-bit cells at 2^(sg - sh).  Returns the tile's exact total at
+// the scale 2^(sg - sh) (valid in thread 0).
+template <int N, int MAS, int G, bool WIDE>
+__device__ __forceinline__ long long tile_grid(const DepGeom& g, const float4* __restrict__ entries, unsigned beg,
+                                               unsigned end, int sg, int sh, int grid, int x0, int y0,
+                                               const float2* __restrict__ tw, float2* __restrict__ spec,
+                                               unsigned char* smem, long long* s_part) {
+  using CT = ColTile<N>;
+  using Cell = typename std::conditional<WIDE, unsigned long long, int>::type;
+  constexpr int R = MAS, TX = CT::TX, TY = CT::TY, NPEN = CT::NPEN, PAIRS = CT::PAIRS, NT = CT::NT;
+  constexpr int P = N / 2 + 8, H = N / 2;
+  Cell* acc = reinterpret_cast<Cell*>(smem);                   // [NPEN][N] fixed-point cells
+  float4* cs4 = reinterpret_cast<float4*>(smem);               // [PAIRS/2][N] slots of two columns, alias the cells
+  const int tid = threadIdx.x;
+  const int s = sg - sh;
+  // 2^s and 2^-s as two exact power-of-two factors each (s may reach -130); 2^-s is one normal
+  // float unless s < -126 (weights beyond 2^150)
+  const float up1 = ldexpf(1.0f, s / 2), up2 = ldexpf(1.0f, s - s / 2);
+  const bool one_dn = s >= -126;
+  const float dn1 = one_dn ? ldexpf(1.0f, -s) : ldexpf(1.0f, -(s / 2));
+  const float dn2 = one_dn ? 1.0f : ldexpf(1.0f, -(s - s / 2));
+  const long long gstride = (long long)N * N * P;
+
+  {
+    uint4* a4 = reinterpret_cast<uint4*>(acc);
+    for (int k = tid; k < (int)(NPEN * N * sizeof(Cell) / 16); k += NT) a4[k] = make_uint4(0u, 0u, 0u, 0u);
+  }
+  __syncthreads();
+  for (unsigned i = beg + tid; i < end; i += NT) {
+    const float4 e = entries[i];
+    Axis<R> ax, ay, az;
+    make_axis<MAS, 0>(g, e.x, grid, ax);
+    make_axis<MAS, 0>(g, e.y, grid, ay);
+    make_axis<MAS, 0>(g, e.z, grid, az);
+    int lx[R], ly[R], zz[R];
+    local_nodes<R>(ax, N, x0, TX, lx);
+    local_nodes<R>(ay, N, y0, TY, ly);
+    const float wsc = __fmul_rn(__fmul_rn(e.w, up1), up2);   // exact: powers of two
+    float wz[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      zz[r] = wrapn(az.first + r, N);
+      wz[r] = __fmul_rn(az.w[r], wsc);
+    }
+#pragma unroll
+    for (int rx = 0; rx < R; ++rx) {
+      if (lx[rx] < 0) continue;
+#pragma unroll
+      for (int ry = 0; ry < R; ++ry) {
+        if (ly[ry] < 0) continue;
+        const float wxy = __fmul_rn(ax.w[rx], ay.w[ry]);
+        const int row = (lx[rx] * TY + ly[ry]) * N;
+#pragma unroll
+        for (int rz = 0; rz < R; ++rz) {
+          const int v = __float2int_rn(__fmul_rn(wxy, wz[rz]));
+          if constexpr (WIDE) atomicAdd(&acc[row + zz[rz]], (unsigned long long)(long long)v);
+          else atomicAdd(&acc[row + zz[rz]], v);
+        }
+      }
+    }
+  }
+  __syncthreads();
+
+  // z transform: pencils 2q and 2q+1 are the real and imaginary parts of
+  // column q; a thread transforms columns 2cp and 2cp+1 (pencils 4cp..4cp+3)
+  long long part = 0;
+  auto gin = [&part, one_dn, dn1, dn2, acc](int j, int cp) {
+    float v[4];
+#pragma unroll
+    for (int f = 0; f < 4; ++f) {
+      const long long q = (long long)acc[(4 * cp + f) * N + j];
+      part += q;
+      v[f] = __fmul_rn(WIDE ? __ll2float_rn(q) : __int2float_rn((int)q), dn1);   // exact: a power of two
+      if (!one_dn) v[f] = __fmul_rn(v[f], dn2);
+    }
+    return make_float4(v[0], v[1], v[2], v[3]);
+  };
+  auto sin_ = [cs4](int j, int cp) { return cs4[cp * N + fft::zsw(j)]; };
+  auto sout = [cs4](int j, int cp, float4 v) { cs4[cp * N + fft::zsw(j)] = v; };
+  // N = 512, 32-bit cells: every stage is radix 8 and the 64 threads of a column pair own its data
+  // (the first stage's writes alias the pair's own pencils), so the stages synchronise 64-thread
+  // groups only.  64-bit cells span twice the bytes of the complex slots: whole-CTA barriers.
+  constexpr int GS = (!WIDE && N == 512 && NT == PAIRS / 2 * (N / 8)) ? N / 8 : 0;
+  fft::run_stages2<N, PAIRS / 2, NT, true, true, true, decltype(gin), decltype(sin_), decltype(sout),
+                   decltype(sout), GS>(gin, sin_, sout, sout, tw, tid);
+
+  // split the packed spectra; write all pencils' rows (row padding -> 0)
+  const float2* cs = reinterpret_cast<const float2*>(cs4);
+  float2* out = spec + grid * gstride;
+  for (int idx = tid; idx < PAIRS * P; idx += NT) {
+    const int q = idx / P, k = idx - (idx / P) * P;
+    float2 a = make_float2(0.f, 0.f), b = make_float2(0.f, 0.f);
+    if (k <= H) {
+      const float2 c = cs[((q >> 1) * N + fft::zsw(k)) * 2 + (q & 1)];
+      const float2 m = cs[((q >> 1) * N + fft::zsw((N - k) & (N - 1))) * 2 + (q & 1)];
+      const float2 cm = make_float2(m.x, -m.y);
+      const float2 sum = fft::cadd(c, cm), dif = fft::cmi(fft::csub(c, cm));
+      a = make_float2(0.5f * sum.x, 0.5f * sum.y);
+      b = make_float2(0.5f * dif.x, 0.5f * dif.y);
+    }
+    const int f0 = 2 * q, f1 = 2 * q + 1;
+    const long long r0 = (long long)(x0 + f0 / TY) * N + (y0 + f0 % TY);
+    const long long r1 = (long long)(x0 + f1 / TY) * N + (y0 + f1 % TY);
+    __stcs(out + r0 * P + k, a);
+    __stcs(out + r1 * P + k, b);
+  }
+
+  // the tile's exact total
+  for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+  if ((tid & 31) == 0) s_part[tid >> 5] = part;
+  __syncthreads();                                     // also: the next grid reuses the accumulators
+  long long tm = 0;
+  if (tid == 0)
+    for (int k = 0; k < NT / 32; ++k) tm += s_part[k];
+  return tm;
+}
 
 template <int N, int MAS, int G>
 __global__ void __launch_bounds__(ColTile<N>::NT, ColTile<N>::MINB)
@@ -55,11 +186,8 @@ deposit_fftz_kernel(DepGeom g, const float4* __restrict__ entries, const unsigne
                     const unsigned* __restrict__ offsets, const DepCounters* ctr, const float2* __restrict__ tw,
                     float2* __restrict__ spec, long long* __restrict__ tile_mass) {
   using CT = ColTile<N>;
-  constexpr int R = MAS, TX = CT::TX, TY = CT::TY, NPEN = CT::NPEN, PAIRS = CT::PAIRS, NT = CT::NT;
-  constexpr int P = N / 2 + 8, H = N / 2;
+  constexpr int R = MAS, TX = CT::TX, TY = CT::TY, NPEN = CT::NPEN, NT = CT::NT;
   extern __shared__ __align__(16) int acc_smem[];
-  int* acc = acc_smem;                                 // [NPEN][N] fixed-point cells
-  float4* cs4 = reinterpret_cast<float4*>(acc);        // [PAIRS/2][N] slots of two columns, alias the cells
   int* zc = acc_smem + NPEN * N;                       // [N] entries whose stencil (any grid) covers plane z
   __shared__ long long s_part[NT / 32];
   __shared__ int s_max[NT / 32];
@@ -99,100 +227,62 @@ deposit_fftz_kernel(DepGeom g, const float4* __restrict__ entries, const unsigne
   // a node weight of TSC (<= 0.75^3) or PCS (<= (2/3)^3) is below 1/2: one more bit
   constexpr int WBIT = (MAS == GBP_TSC || MAS == GBP_PCS) ? 1 : 0;
   const int sh = lg > WBIT ? lg - WBIT : 0;            // tile scale 2^s = 2^(sg - sh), never finer than 2^sg
-  const int s = sg - sh;
-  // 2^s and 2^-s as two exact power-of-two factors each (s may reach -130)
-  const float up1 = ldexpf(1.0f, s / 2), up2 = ldexpf(1.0f, s - s / 2);
-  const float dn1 = ldexpf(1.0f, -(s / 2)), dn2 = ldexpf(1.0f, -(s - s / 2));
-  const long long gstride = (long long)N * N * P;
-
+  if (sh > SH_MAX) {                                   // a dense clump: the wide kernel takes this tile
+    if (tid == 0) tile_mass[t] = WIDE_MARK;
+    return;
+  }
   for (int grid = 0; grid < G; ++grid) {
-    {
-      uint4* a4 = reinterpret_cast<uint4*>(acc);
-      for (int k = tid; k < NPEN * N / 4; k += NT) a4[k] = make_uint4(0u, 0u, 0u, 0u);
-    }
-    __syncthreads();
-    for (unsigned i = beg + tid; i < end; i += NT) {
-      const float4 e = entries[i];
-      Axis<R> ax, ay, az;
-      make_axis<MAS, 0>(g, e.x, grid, ax);
-      make_axis<MAS, 0>(g, e.y, grid, ay);
-      make_axis<MAS, 0>(g, e.z, grid, az);
-      int lx[R], ly[R], zz[R];
-      local_nodes<R>(ax, N, x0, TX, lx);
-      local_nodes<R>(ay, N, y0, TY, ly);
-      const float wsc = __fmul_rn(__fmul_rn(e.w, up1), up2);   // exact: powers of two
-      float wz[R];
-#pragma unroll
-      for (int r = 0; r < R; ++r) {
-        zz[r] = wrapn(az.first + r, N);
-        wz[r] = __fmul_rn(az.w[r], wsc);
+    const long long tm = tile_grid<N, MAS, G, false>(g, entries, beg, end, sg, sh, grid, x0, y0, tw, spec,
+                                                     reinterpret_cast<unsigned char*>(acc_smem), s_part);
+    if (tid == 0) tile_mass[(long long)grid * gridDim.x + t] = tm * (1LL << sh);   // exact, at the common scale 2^sg
+  }
+}
+
+// The tiles deposit_fftz_kernel left (tile_mass entry WIDE_MARK): 64-bit
+// cells at the common scale.  Persistent: CTA b owns a contiguous range of
+// tiles, finds its marked ones with one parallel scan (such tiles are rare;
+// with none, that scan is all a CTA does) and processes them in turn.
+constexpr int WIDE_LIST = 64;                          // marked tiles listed per scan round
+
+template <int N, int MAS, int G>
+__global__ void __launch_bounds__(ColTile<N>::NT, 1)
+deposit_fftz_wide_kernel(DepGeom g, const float4* __restrict__ entries, const unsigned* __restrict__ counts,
+                         const unsigned* __restrict__ offsets, const DepCounters* ctr, const float2* __restrict__ tw,
+                         float2* __restrict__ spec, long long* __restrict__ tile_mass, int ntiles) {
+  using CT = ColTile<N>;
+  constexpr int NT = CT::NT;
+  extern __shared__ __align__(16) unsigned long long wide_smem[];
+  __shared__ long long s_part[NT / 32];
+  __shared__ int s_list[WIDE_LIST];
+  __shared__ int s_n;
+  const int sg = fixed_scale_exp(ctr->maxw_bits, 0);
+  const int per = (ntiles + gridDim.x - 1) / gridDim.x;
+  const int t0 = blockIdx.x * per, t1 = min(ntiles, t0 + per);
+  for (int base = t0; base < t1; base += NT) {
+    for (;;) {                                         // list the marked tiles of [base, base + NT), 64 at a time
+      if (threadIdx.x == 0) s_n = 0;
+      __syncthreads();
+      const int t = base + (int)threadIdx.x;
+      if (t < t1 && tile_mass[t] == WIDE_MARK) {
+        const int k = atomicAdd(&s_n, 1);
+        if (k < WIDE_LIST) s_list[k] = t;
       }
-#pragma unroll
-      for (int rx = 0; rx < R; ++rx) {
-        if (lx[rx] < 0) continue;
-#pragma unroll
-        for (int ry = 0; ry < R; ++ry) {
-          if (ly[ry] < 0) continue;
-          const float wxy = __fmul_rn(ax.w[rx], ay.w[ry]);
-          const int row = (lx[rx] * TY + ly[ry]) * N;
-#pragma unroll
-          for (int rz = 0; rz < R; ++rz) atomicAdd(&acc[row + zz[rz]], __float2int_rn(__fmul_rn(wxy, wz[rz])));
+      __syncthreads();
+      const int n = min(s_n, WIDE_LIST);
+      if (n == 0) break;                               // uniform over the CTA
+      for (int k = 0; k < n; ++k) {
+        const int tt = s_list[k];
+        const int ty = tt % g.nt[1], tx = tt / g.nt[1];
+        const unsigned beg = offsets[tt];
+        const unsigned end = beg + counts[tt * CSTRIDE];
+        for (int grid = 0; grid < G; ++grid) {
+          const long long tm = tile_grid<N, MAS, G, true>(g, entries, beg, end, sg, 0, grid, tx * CT::TX,
+                                                          ty * CT::TY, tw, spec,
+                                                          reinterpret_cast<unsigned char*>(wide_smem), s_part);
+          if (threadIdx.x == 0) tile_mass[(long long)grid * ntiles + tt] = tm;   // clears the mark
         }
       }
-    }
-    __syncthreads();
-
-    // z transform: pencils 2q and 2q+1 are the real and imaginary parts of
-    // column q; a thread transforms columns 2cp and 2cp+1 (pencils 4cp..4cp+3)
-    long long part = 0;
-    auto gin = [&part, dn1, dn2, acc](int j, int cp) {
-      float v[4];
-#pragma unroll
-      for (int f = 0; f < 4; ++f) {
-        const int q = acc[(4 * cp + f) * N + j];
-        part += q;
-        v[f] = __fmul_rn(__fmul_rn(__int2float_rn(q), dn1), dn2);
-      }
-      return make_float4(v[0], v[1], v[2], v[3]);
-    };
-    auto sin_ = [cs4](int j, int cp) { return cs4[cp * N + fft::zsw(j)]; };
-    auto sout = [cs4](int j, int cp, float4 v) { cs4[cp * N + fft::zsw(j)] = v; };
-    // N = 512: every stage is radix 8 and the 64 threads of a column pair own
-    // its data (the first stage's writes alias the pair's own pencils), so
-    // the stages synchronise 64-thread groups only
-    constexpr int GS = (N == 512 && NT == PAIRS / 2 * (N / 8)) ? N / 8 : 0;
-    fft::run_stages2<N, PAIRS / 2, NT, true, true, true, decltype(gin), decltype(sin_), decltype(sout),
-                     decltype(sout), GS>(gin, sin_, sout, sout, tw, tid);
-
-    // split the packed spectra; write all pencils' rows (row padding -> 0)
-    const float2* cs = reinterpret_cast<const float2*>(cs4);
-    float2* out = spec + grid * gstride;
-    for (int idx = tid; idx < PAIRS * P; idx += NT) {
-      const int q = idx / P, k = idx - (idx / P) * P;
-      float2 a = make_float2(0.f, 0.f), b = make_float2(0.f, 0.f);
-      if (k <= H) {
-        const float2 c = cs[((q >> 1) * N + fft::zsw(k)) * 2 + (q & 1)];
-        const float2 m = cs[((q >> 1) * N + fft::zsw((N - k) & (N - 1))) * 2 + (q & 1)];
-        const float2 cm = make_float2(m.x, -m.y);
-        const float2 sum = fft::cadd(c, cm), dif = fft::cmi(fft::csub(c, cm));
-        a = make_float2(0.5f * sum.x, 0.5f * sum.y);
-        b = make_float2(0.5f * dif.x, 0.5f * dif.y);
-      }
-      const int f0 = 2 * q, f1 = 2 * q + 1;
-      const long long r0 = (long long)(x0 + f0 / TY) * N + (y0 + f0 % TY);
-      const long long r1 = (long long)(x0 + f1 / TY) * N + (y0 + f1 % TY);
-      __stcs(out + r0 * P + k, a);
-      __stcs(out + r1 * P + k, b);
-    }
-
-    // this tile's exact total at the common scale 2^sg (read by stats_kernel)
-    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-    if ((tid & 31) == 0) s_part[tid >> 5] = part;
-    __syncthreads();                                   // also: the next grid reuses the accumulators
-    if (tid == 0) {
-      long long tm = 0;
-      for (int k = 0; k < NT / 32; ++k) tm += s_part[k];
-      tile_mass[(long long)grid * gridDim.x + t] = tm * (1LL << sh);   // exact, at the common scale 2^sg
+      __syncthreads();                                 // the marks are replaced before the next scan
     }
   }
 }
@@ -242,8 +332,21 @@ int run_fused(const DepGeom& g, const DepLayout& L, const DepBuffers& b, const f
   auto k = deposit_fftz_kernel<N, MAS, G>;
   const size_t smem = ColTile<N>::SMEM;
   GBP_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  GBP_TRACE("deposit_fft_z", st);
-  k<<<L.ntiles, ColTile<N>::NT, smem, st>>>(g, b.entries, b.counts, b.offsets, b.ctr, tw, spec, b.tile_mass);
+  {
+    GBP_TRACE("deposit_fft_z", st);
+    k<<<L.ntiles, ColTile<N>::NT, smem, st>>>(g, b.entries, b.counts, b.offsets, b.ctr, tw, spec, b.tile_mass);
+    GBP_LAUNCH_CHECK();
+  }
+  // tiles of dense clumps, if any, with 64-bit cells (one CTA per SM scans the marks)
+  auto kw = deposit_fftz_wide_kernel<N, MAS, G>;
+  const size_t smem_w = ColTile<N>::SMEM_WIDE;
+  GBP_CUDA_TRY(cudaFuncSetAttribute(kw, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_w));
+  int dev = 0, sms = 0;
+  GBP_CUDA_TRY(cudaGetDevice(&dev));
+  GBP_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  GBP_TRACE("deposit_fft_z_wide", st);
+  kw<<<std::max(1, std::min(sms, L.ntiles)), ColTile<N>::NT, smem_w, st>>>(g, b.entries, b.counts, b.offsets, b.ctr,
+                                                                          tw, spec, b.tile_mass, L.ntiles);
   GBP_LAUNCH_CHECK();
   return GBP_OK;
 }

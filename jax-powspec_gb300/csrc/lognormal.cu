@@ -237,9 +237,20 @@ extern "C" int gbp_lognormal_workspace_size(int grid, size_t* bytes) {
   return GBP_OK;
 }
 
-extern "C" int gbp_lognormal(int grid, double box, double k_cut, double sigma_v, int64_t n, unsigned long long seed,
-                             float* x, float* y, float* z, void* workspace, size_t ws_bytes, gbp_stream_t stream_) {
-  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream_);
+namespace gbp {
+namespace {
+
+// rho = exp(g - 1/2) as float32, for gbp_lognormal_field
+__global__ void rho_out_kernel(const float* g, float* rho, long long cells) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < cells) rho[i] = (float)exp((double)g[i] - 0.5);
+}
+
+// Steps 1-5 (n = 0: steps 1-3 and the prefix sum only).  g_out / rho_out,
+// when given, receive the Gaussian field g and rho = 1 + delta_LN.
+int lognormal_run(int grid, double box, double k_cut, double sigma_v, int64_t n, unsigned long long seed, float* x,
+                  float* y, float* z, float* g_out, float* rho_out, void* workspace, size_t ws_bytes,
+                  cudaStream_t st) {
   if (grid < 4 || grid > 1024 || (grid & 1) || !(box > 0.0) || !(k_cut > 0.0) || sigma_v < 0.0 || n < 0)
     return GBP_ERR_INVALID;
   if (n > 0 && (!x || !y || !z)) return GBP_ERR_INVALID;
@@ -278,6 +289,12 @@ extern "C" int gbp_lognormal(int grid, double box, double k_cut, double sigma_v,
   if (cufftSetStream(c2r, st) != CUFFT_SUCCESS || cufftSetWorkArea(c2r, fws) != CUFFT_SUCCESS ||
       cufftExecC2R(c2r, reinterpret_cast<cufftComplex*>(spec), eps) != CUFFT_SUCCESS)
     return fail(GBP_ERR_CUFFT);
+  if (g_out && cudaMemcpyAsync(g_out, eps, (size_t)cells * 4, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+    return fail(GBP_ERR_CUDA);
+  if (rho_out) {
+    rho_out_kernel<<<(unsigned)((cells + 255) / 256), 256, 0, st>>>(eps, rho_out, cells);
+    if (cudaGetLastError() != cudaSuccess) return fail(GBP_ERR_CUDA);
+  }
   {
     GBP_TRACE("lognormal_density", st);
     density_kernel<<<(unsigned)((cells + 255) / 256), 256, 0, st>>>(eps, cdf, cells);
@@ -293,4 +310,20 @@ extern "C" int gbp_lognormal(int grid, double box, double k_cut, double sigma_v,
   }
   // cuFFT plans can be destroyed once their work is enqueued
   return fail(GBP_OK);
+}
+
+}  // namespace
+}  // namespace gbp
+
+extern "C" int gbp_lognormal(int grid, double box, double k_cut, double sigma_v, int64_t n, unsigned long long seed,
+                             float* x, float* y, float* z, void* workspace, size_t ws_bytes, gbp_stream_t stream) {
+  return lognormal_run(grid, box, k_cut, sigma_v, n, seed, x, y, z, nullptr, nullptr, workspace, ws_bytes,
+                       reinterpret_cast<cudaStream_t>(stream));
+}
+
+extern "C" int gbp_lognormal_field(int grid, double box, double k_cut, unsigned long long seed, float* g_out,
+                                   float* rho_out, void* workspace, size_t ws_bytes, gbp_stream_t stream) {
+  if (!g_out && !rho_out) return GBP_ERR_INVALID;
+  return lognormal_run(grid, box, k_cut, 0.0, 0, seed, nullptr, nullptr, nullptr, g_out, rho_out, workspace, ws_bytes,
+                       reinterpret_cast<cudaStream_t>(stream));
 }

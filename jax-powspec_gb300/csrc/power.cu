@@ -290,38 +290,23 @@ int power_layout(const gbp_bins_s* B, int G, int ells, int Lzs, PowLayout& L) {
   return GBP_OK;
 }
 
-}  // namespace
-}  // namespace gbp
-
-using namespace gbp;
-
-extern "C" int gbp_power_workspace_size(gbp_bins bins, int G, int z_pitch, int ells, size_t* bytes) {
-  if (!bins || !bytes || (G != 1 && G != 2)) return GBP_ERR_INVALID;
-  PowLayout L;
-  const int st = power_layout(bins, G, ells, z_pitch > 0 ? z_pitch : bins->N / 2 + 1, L);
-  if (st) return st;
-  *bytes = L.ws_total;
-  return GBP_OK;
-}
-
-extern "C" int gbp_power(const void* spectrum, int G, int z_pitch, gbp_bins B, int mas_order, int ells,
-                         const double* mass, double* sums_out, long long* nmodes_out, double* ksum_out,
-                         void* workspace, size_t ws_bytes, gbp_stream_t stream_) {
-  cudaStream_t stream = reinterpret_cast<cudaStream_t>(stream_);
+// Argument checks shared by gbp_power and gbp_power_noalloc.
+int power_args(const void* spectrum, int G, gbp_bins B, int mas_order, int ells, double* sums_out,
+               long long* nmodes_out, double* ksum_out) {
   if (!spectrum || !B || !sums_out || !nmodes_out) return GBP_ERR_INVALID;
   if (G != 1 && G != 2) return GBP_ERR_INVALID;
   if (mas_order < 0 || mas_order > 8) return GBP_ERR_INVALID;
   if ((ells & (GBP_ELL0 | GBP_ELL2 | GBP_ELL4)) == 0 || (ells & ~15)) return GBP_ERR_INVALID;
   if ((ells & GBP_KSUM) && !ksum_out) return GBP_ERR_INVALID;
-  const int Lzs = z_pitch > 0 ? z_pitch : B->N / 2 + 1;
-  PowLayout L;
-  int st = power_layout(B, G, ells, Lzs, L);
-  if (st) return st;
-  if (!workspace || ws_bytes < L.ws_total) return GBP_ERR_WORKSPACE;
+  return GBP_OK;
+}
 
-  Carver cv(workspace);
-  float2* part_ff = cv.take<float2>((size_t)L.C * L.NV * B->nbe);
-
+// The binning launches of gbp_power and gbp_power_noalloc: the persistent
+// binning kernel writes the per-group float-float partials to part_ff
+// (L.C * L.NV * nbe float2), then one block per bin folds them.
+int launch_power(const void* spectrum, int G, int Lzs, gbp_bins B, int mas_order, int ells, const double* mass,
+                 double* sums_out, long long* nmodes_out, double* ksum_out, const PowLayout& L, float2* part_ff,
+                 cudaStream_t stream) {
   PowGeom g;
   g.s0 = static_cast<const float2*>(spectrum);
   g.s1 = G == 2 ? g.s0 + L.total : nullptr;
@@ -375,6 +360,36 @@ extern "C" int gbp_power(const void* spectrum, int G, int z_pitch, gbp_bins B, i
   return GBP_OK;
 }
 
+}  // namespace
+}  // namespace gbp
+
+using namespace gbp;
+
+extern "C" int gbp_power_workspace_size(gbp_bins bins, int G, int z_pitch, int ells, size_t* bytes) {
+  if (!bins || !bytes || (G != 1 && G != 2)) return GBP_ERR_INVALID;
+  PowLayout L;
+  const int st = power_layout(bins, G, ells, z_pitch > 0 ? z_pitch : bins->N / 2 + 1, L);
+  if (st) return st;
+  *bytes = L.ws_total;
+  return GBP_OK;
+}
+
+extern "C" int gbp_power(const void* spectrum, int G, int z_pitch, gbp_bins B, int mas_order, int ells,
+                         const double* mass, double* sums_out, long long* nmodes_out, double* ksum_out,
+                         void* workspace, size_t ws_bytes, gbp_stream_t stream_) {
+  int st = power_args(spectrum, G, B, mas_order, ells, sums_out, nmodes_out, ksum_out);
+  if (st) return st;
+  const int Lzs = z_pitch > 0 ? z_pitch : B->N / 2 + 1;
+  PowLayout L;
+  st = power_layout(B, G, ells, Lzs, L);
+  if (st) return st;
+  if (!workspace || ws_bytes < L.ws_total) return GBP_ERR_WORKSPACE;
+  Carver cv(workspace);
+  float2* part_ff = cv.take<float2>((size_t)L.C * L.NV * B->nbe);
+  return launch_power(spectrum, G, Lzs, B, mas_order, ells, mass, sums_out, nmodes_out, ksum_out, L, part_ff,
+                      reinterpret_cast<cudaStream_t>(stream_));
+}
+
 extern "C" int gbp_power_normalize(const double* sums, const long long* nmodes, const double* ksum, int nb, int N,
                                    double box, const double* mass, const gbp_deposit_stats* stats,
                                    int subtract_shot, double* pk_out, double* kmean_out, gbp_stream_t stream_) {
@@ -407,8 +422,9 @@ extern "C" int gbp_power_normalize_job(const double* sums, const long long* nmod
 // ---------------------------------------------------------------------------
 // Allocation-free binning.  Some callers cannot allocate device memory when
 // they call in: a JAX/XLA custom call (the way a JAX program would reach
-// this path) is handed only its operand and result buffers, and a host thread
-// that is recording the stream into a CUDA graph may not call cudaMalloc.
+// this path) is handed only its operand and result buffers, and its device
+// memory belongs to JAX's allocator, which reserves most of the GPU up front,
+// so a cudaMalloc of the library's own can fail or compete with it.
 // gbp_power_noalloc is gbp_power with its scratch (the per-group float-float
 // partial sums) in a fixed device array owned by the library, so the caller
 // passes only inputs and outputs.
@@ -457,71 +473,16 @@ int noalloc_partials(float2** out) {
 extern "C" int gbp_power_noalloc(const void* spectrum, int G, int z_pitch, gbp_bins B, int mas_order, int ells,
                                  const double* mass, double* sums_out, long long* nmodes_out, double* ksum_out,
                                  gbp_stream_t stream_) {
-  cudaStream_t stream = reinterpret_cast<cudaStream_t>(stream_);
-  if (!spectrum || !B || !sums_out || !nmodes_out) return GBP_ERR_INVALID;
-  if (G != 1 && G != 2) return GBP_ERR_INVALID;
-  if (mas_order < 0 || mas_order > 8) return GBP_ERR_INVALID;
-  if ((ells & (GBP_ELL0 | GBP_ELL2 | GBP_ELL4)) == 0 || (ells & ~15)) return GBP_ERR_INVALID;
-  if ((ells & GBP_KSUM) && !ksum_out) return GBP_ERR_INVALID;
+  int st = power_args(spectrum, G, B, mas_order, ells, sums_out, nmodes_out, ksum_out);
+  if (st) return st;
   const int Lzs = z_pitch > 0 ? z_pitch : B->N / 2 + 1;
   PowLayout L;
-  int st = power_layout(B, G, ells, Lzs, L);
+  st = power_layout(B, G, ells, Lzs, L);
   if (st) return st;
   if ((size_t)L.C * L.NV * B->nbe > GBP_NOALLOC_PARTIALS) return GBP_ERR_UNSUPPORTED;
   float2* part_ff = nullptr;
   st = noalloc_partials(&part_ff);
   if (st) return st;
-
-  PowGeom g;
-  g.s0 = static_cast<const float2*>(spectrum);
-  g.s1 = G == 2 ? g.s0 + L.total : nullptr;
-  g.N = B->N;
-  g.Lz = B->N / 2 + 1;
-  g.Lzs = Lzs;
-  g.total = L.total;
-  g.chunk = L.chunk;
-  g.nb = B->nb;
-  g.nbe = B->nbe;
-  g.tu = B->last_closed;
-  g.lut_shift = B->lut_shift;
-  g.lut_n = B->lut_n;
-  g.mas_order = mas_order;
-  g.thr = B->d_thr;
-  g.lut = B->d_lut;
-  g.inv_sinc2 = B->d_inv_sinc2;
-  g.eph = B->d_eph;
-  g.zero_dc = mass != nullptr;
-  g.part_ff = part_ff;
-  g.warps = L.warps;
-  const bool aligned = ((reinterpret_cast<uintptr_t>(g.s0) | reinterpret_cast<uintptr_t>(g.s1)) & 15u) == 0;
-  const bool wide = L.wide && aligned;
-  void (*kern)(PowGeom) = nullptr;
-  const bool inter = G == 2;
-  if (L.NV == 1)
-    kern = wide ? (inter ? power_kernel<1, true, true> : power_kernel<1, false, true>)
-                : (inter ? power_kernel<1, true, false> : power_kernel<1, false, false>);
-  else if (L.NV == 2)
-    kern = wide ? (inter ? power_kernel<2, true, true> : power_kernel<2, false, true>)
-                : (inter ? power_kernel<2, true, false> : power_kernel<2, false, false>);
-  else
-    kern = wide ? (inter ? power_kernel<3, true, true> : power_kernel<3, false, true>)
-                : (inter ? power_kernel<3, true, false> : power_kernel<3, false, false>);
-  GBP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem));
-  int dev = 0, sms = 0, per_sm = 0;
-  GBP_CUDA_TRY(cudaGetDevice(&dev));
-  GBP_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  GBP_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, L.warps * 32, L.smem));
-  g.groups = L.C;
-  const int grid = std::max(1, std::min(L.C, sms * std::max(per_sm, 1)));
-  {
-    GBP_TRACE("power_bins", stream);
-    kern<<<grid, L.warps * 32, L.smem, stream>>>(g);
-    GBP_LAUNCH_CHECK();
-  }
-  GBP_TRACE("power_reduce", stream);
-  power_reduce_kernel<<<B->nb, FOLD_THREADS, 0, stream>>>(
-      part_ff, L.C, L.NV, B->nb, B->nbe, B->d_nmodes, B->d_ksum, sums_out, nmodes_out,
-      (ells & GBP_KSUM) ? ksum_out : nullptr);
-  GBP_LAUNCH_CHECK();
-  return GBP_OK;
+  return launch_power(spectrum, G, Lzs, B, mas_order, ells, mass, sums_out, nmodes_out, ksum_out, L, part_ff,
+                      reinterpret_cast<cudaStream_t>(stream_));
 }

@@ -117,6 +117,7 @@ SIGNATURES = [
     ("gbp_particles_power_job", _i, [_vp, _i64, _vp, _vp, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     ("gbp_lognormal_workspace_size", _i, [_i, C.POINTER(_sz)]),
     ("gbp_lognormal", _i, [_i, _d, _d, _d, _i64, C.c_ulonglong, _vp, _vp, _vp, _vp, _sz, _vp]),
+    ("gbp_lognormal_field", _i, [_i, _d, _d, C.c_ulonglong, _vp, _vp, _vp, _sz, _vp]),
     ("gbp_philox4x32_10", _i, [_vp, _vp, _vp]),
     ("gbp_xi_workspace_size", _i, [_vp, _vp, C.POINTER(_sz)]),
     ("gbp_xi", _i, [_vp, _vp, _vp, _vp, _vp, _i, _i, _vp, _vp, _vp, _sz, _vp]),

@@ -4,7 +4,8 @@
 ``powspec_vec_fundamental(delta, box_size)`` keep the reference's signatures
 and return tuples ``(k3D, Pk3D, Nmodes3D)`` as float32 CUDA tensors:
 
-* the mesh is FFT'd with cuFFT (R2C), then one fused kernel applies the CIC
+* the mesh is FFT'd (R2C) by the library's own transform for power-of-two
+  sides 64..1024 and by cuFFT otherwise, then one fused kernel applies the CIC
   window correction (1/sinc)^2 per axis (src/correlations.py:20-21,32,39),
   squares, weights by L_0, L_2, L_4 of mu = kz/k (:36-38,45-47) and bins;
 * binning reproduces jnp.histogram on k = sqrtf(kx^2+ky^2+kz^2) against the

@@ -31,7 +31,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-__all__ = ["Request", "Result", "Server", "percentiles"]
+__all__ = ["Request", "Result", "Server", "percentiles", "stream_priority"]
 
 
 @dataclass
@@ -224,8 +224,26 @@ class Server:
             self.used -= s.bytes
 
 
+def stream_priority(n_mesh: int) -> int:
+    """CUDA stream priority of a lane (lower is more urgent): small meshes first.
+
+    A 128^3 request takes a fraction of a millisecond on the device and a
+    512^3 one a few milliseconds; at equal priority the small request's
+    kernels wait behind whole waves of the large one's blocks.  With a higher
+    priority the block scheduler starts the small request's blocks as soon as
+    any of the large one's retire, so short requests keep short latencies in
+    a mixed stream.  (Lanes replay CUDA graphs; graph kernels take the
+    priority of the stream they are launched into.)"""
+    if n_mesh <= 128:
+        return -2
+    if n_mesh <= 256:
+        return -1
+    return 0
+
+
 class GpuBackend:
-    """Device side of the server: one native lane + stream + buffers per slot."""
+    """Device side of the server: one native lane + stream + buffers per slot; lanes of small meshes
+    run on higher-priority streams (stream_priority)."""
 
     def __init__(self, device=None):
         import torch
@@ -275,7 +293,7 @@ class _GpuLane:
         self.km_host = torch.empty((1, nb), dtype=torch.float64, pin_memory=True)
         self.nm_host = torch.empty((1, nb), dtype=torch.int64, pin_memory=True)
         self.st_host = torch.empty((1, _lib.STATS_BYTES), dtype=torch.uint8, pin_memory=True)
-        self.stream = torch.cuda.Stream(device=dev)
+        self.stream = torch.cuda.Stream(device=dev, priority=stream_priority(req.n_mesh))
         self.event = torch.cuda.Event()
         self.event.record(self.stream)
         self.kedges = self.runner.kedges_grid

@@ -17,7 +17,8 @@ from __future__ import annotations
 
 import numpy as np
 
-__all__ = ["uniform_catalogue", "lognormal_catalogue", "lognormal_density", "lognormal_catalogue_gpu"]
+__all__ = ["uniform_catalogue", "lognormal_catalogue", "lognormal_density", "lognormal_catalogue_gpu",
+           "lognormal_field_gpu", "gaussian_power"]
 
 
 def _clamp_box(a: np.ndarray, box: float) -> np.ndarray:
@@ -104,3 +105,42 @@ def lognormal_catalogue_gpu(n: int, box: float, grid: int = 256, seed: int = 0, 
                                  _native._stream_of(dev)), "gbp_lognormal")
     return x[:n], y[:n], z[:n]
 
+
+def gaussian_power(k, box: float, grid: int, k_cut: float = 0.3) -> np.ndarray:
+    """P_G(k) = A k exp(-(k/k_cut)^2) of the generators, A set so that the lattice variance
+    sum_k P_G(k) / V over the grid^3 lattice is 1 (h^-3 Mpc^3; k in h/Mpc)."""
+    kf = 2 * np.pi / box
+    ki = np.fft.fftfreq(grid, d=1.0 / grid) * kf
+    kz = np.fft.rfftfreq(grid, d=1.0 / grid) * kf
+    kk = np.sqrt(ki[:, None, None] ** 2 + ki[None, :, None] ** 2 + kz[None, None, :] ** 2)
+    shape = kk * np.exp(-((kk / k_cut) ** 2))
+    weight = np.full(kk.shape, 2.0)
+    weight[..., 0] = 1.0
+    if grid % 2 == 0:
+        weight[..., -1] = 1.0
+    A = box ** 3 / (weight * shape).sum()
+    k = np.asarray(k, dtype=np.float64)
+    return A * k * np.exp(-((k / k_cut) ** 2))
+
+
+def lognormal_field_gpu(grid: int, box: float, seed: int = 0, k_cut: float = 0.3, device=None):
+    """(g, rho): the device generator's Gaussian field and rho = exp(g - 1/2) = 1 + delta_LN on the
+    grid^3 lattice (float32 CUDA tensors [grid, grid, grid]), the field lognormal_catalogue_gpu samples
+    its particles from for the same (grid, box, seed, k_cut)."""
+    import ctypes as C
+
+    import torch
+
+    from . import _lib, _native
+    dev = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
+    lib = _lib.load()
+    need = C.c_size_t(0)
+    _lib.check(lib.gbp_lognormal_workspace_size(int(grid), C.byref(need)), "gbp_lognormal_workspace_size")
+    ws = _native.workspace(need.value, dev)
+    g = torch.empty((grid, grid, grid), dtype=torch.float32, device=dev)
+    rho = torch.empty_like(g)
+    _lib.check(lib.gbp_lognormal_field(int(grid), float(box), float(k_cut), int(seed) & 0xFFFFFFFFFFFFFFFF,
+                                       C.c_void_p(g.data_ptr()), C.c_void_p(rho.data_ptr()),
+                                       C.c_void_p(ws.data_ptr()), ws.numel(), _native._stream_of(dev)),
+               "gbp_lognormal_field")
+    return g, rho

@@ -7,7 +7,7 @@ here).  Inputs are small and seeded; outputs are written to
 tests/golden/*.npz next to this script.  The GPU tests and the CPU oracle are
 both checked against these files, which never need the reference at run time.
 
-    python tests/golden/make_golden.py [path/to/jax-powspec]
+    python tests/golden/make_golden.py path/to/jax-powspec   (or JAX_POWSPEC_ROOT=...)
 """
 from __future__ import annotations
 
@@ -178,4 +178,7 @@ def main(root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("JAX_POWSPEC_ROOT")
+    if not root:
+        sys.exit("usage: python make_golden.py <path to a jax-powspec checkout>  (or set JAX_POWSPEC_ROOT)")
+    main(root)

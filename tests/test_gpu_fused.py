@@ -17,7 +17,7 @@ def _meshes(N, G, seed):
     return m * 2.0 + 0.5
 
 
-@pytest.mark.parametrize("N", [64, 128, 256])
+@pytest.mark.parametrize("N", [64, 128, 256, 512])
 @pytest.mark.parametrize("G", [1, 2])
 @pytest.mark.parametrize("ells", ["l0", "l02", "l024k"])
 def test_fused_matches_two_step(N, G, ells):
@@ -94,7 +94,7 @@ def test_fused_pipeline_matches_fp64_oracle(mas, interlace):
     np.testing.assert_allclose(res.k_mean.cpu().numpy()[full], ref["kmean"][full], rtol=1e-6)
 
 
-@pytest.mark.parametrize("N", [64, 128, 256])
+@pytest.mark.parametrize("N", [64, 128, 256, 512])
 @pytest.mark.parametrize("mas", ["ngp", "cic", "tsc", "pcs"])
 @pytest.mark.parametrize("G", [1, 2])
 def test_particles_power_matches_mesh_path(N, mas, G):

@@ -1,7 +1,8 @@
 """Precision study: the float32 GPU pipeline against a float64 estimator.
 
-1024^3 meshes, CIC and PCS with interlacing, 16,777,216 lognormal+RSD
-particles (L = 2500), per-bin errors of P_0,2,4 within the target tolerance
+1024^3 meshes, CIC, TSC and PCS with and without interlacing, 16,777,216
+lognormal+RSD particles (L = 2500; also 512^3 with 4,194,304 particles and
+256^3 with 2,000,000), per-bin errors of P_0,2,4 within the target tolerance
 (1e-5 relative for the monopole, 1e-5 of the monopole amplitude for l = 2, 4)
 and bit-exact NGP occupancy counts.  The float64 side is the numpy oracle
 restated with torch on the GPU (tests/fp64_torch.py): the numpy oracle needs
@@ -36,16 +37,16 @@ def _errors(res_pk, ref):
 
 
 @pytest.mark.parametrize("interlace", [False, True])
-@pytest.mark.parametrize("N,n", [(256, 2_000_000), (1024, 16_777_216)])
-def test_precision_cic_pcs_against_fp64(N, n, interlace):
-    _need(40 if N == 1024 else 4)
+@pytest.mark.parametrize("N,n", [(256, 2_000_000), (512, 4_194_304), (1024, 16_777_216)])
+def test_precision_against_fp64(N, n, interlace):
+    _need({256: 4, 512: 12, 1024: 40}[N])
     import fp64_torch as F
     from gbpowspec import PkConfig, PowerSpectrum
     from gbpowspec.batch import shell_edges
     box = 2500.0
     x, y, z = _catalogue(n, box)
     report = {}
-    for mas, order in (("cic", 2), ("pcs", 4)):
+    for mas, order in (("cic", 2), ("tsc", 3), ("pcs", 4)):
         cfg = PkConfig(n_mesh=N, box_size=box, mas=mas, interlace=interlace,
                        k_edges_kf=tuple(shell_edges(N).tolist()))
         ps = PowerSpectrum(cfg)
