@@ -497,7 +497,7 @@ def main():
     cfg = PkConfig(n_mesh=CONFIG["n_mesh"], box_size=CONFIG["box"], mas=CONFIG["mas"],
                    interlace=CONFIG["interlace"], ells=CONFIG["ells"])
     N, G = cfg.n_mesh, cfg.grids
-    ps = PowerSpectrum(cfg, dev)
+    ps = PowerSpectrum(cfg, dev, tiles="auto")          # the autotuner's column tile for this shape
     ps.reserve(n)
     stream = torch.cuda.current_stream(dev)
 
@@ -543,6 +543,8 @@ def main():
     else:
         lanes, lane_rates = tune_lanes(N, jobs, candidates=(1, 2, 3), repeats=1, **kw)
     runner = BatchRunner(N, n_lanes=lanes, device=dev, **kw)
+    from gbpowspec.tune import default_tuner
+    tune_rec = default_tuner().entry(N, cfg.mas, cfg.interlace, n=n, device=dev)
     res = runner.alloc_result(B)
     for _ in range(args.warmup):
         runner.run(jobs, res)
@@ -606,7 +608,9 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded lognormal+RSD mocks)",
         "config": {**_cfg_json(), "path": f"batched: {B} mocks per step over {lanes} lanes (one CUDA graph "
                                           "replay per mock, lanes on their own streams)",
-                   "batch": B, "lanes": lanes, "lane_tuning_mocks_per_s": lane_rates},
+                   "batch": B, "lanes": lanes, "lane_tuning_mocks_per_s": lane_rates,
+                   "column_tile": "%dx%d" % runner.tiles if runner.tiles else None,
+                   "column_tile_tuning_ms_per_mock": (tune_rec or {}).get("ms")},
         "particles_per_s": mocks * n / t_batch,
         "plain": {"value": ws * args.plain_steps / t_plain, "unit": "mocks/s", "steps": args.plain_steps,
                   "ms_per_mock": t_plain / args.plain_steps * 1e3,

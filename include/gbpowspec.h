@@ -275,10 +275,11 @@ int gbp_fft_power(gbp_fft_plan plan, const float* mesh, void* spectrum,
  * of the FFT (library transform sizes: power-of-two meshes 64..1024 and a
  * plan made without the cuFFT override; B-spline deposits).  The mesh is
  * never written: each column tile of pencils is deposited in shared memory
- * (32-bit fixed point at a scale per tile that no cell can overflow, exact
- * and order-independent) and transformed along z there; then the y pass and
- * the x pass fused with the binning.  Interlacing follows the plan (2 grids
- * = interlaced).
+ * (32-bit fixed point at a scale per 4x4-pencil block that no cell can
+ * overflow, exact and order-independent; 64-bit cells for blocks of dense
+ * clumps) and transformed along z there; then the y pass and the x pass
+ * fused with the binning.  Interlacing follows the plan (2 grids =
+ * interlaced); the column tile shape too (gbp_fft_plan_set_tiles).
  * Outputs as gbp_deposit (stats_out, required: it carries the mass the
  * binning and the normalisation use) followed by gbp_fft_power; `spectrum`
  * is scratch of the plan's spectrum size.  Replaces src/mas.py:88-153 +
@@ -286,6 +287,18 @@ int gbp_fft_power(gbp_fft_plan plan, const float* mesh, void* spectrum,
 int gbp_particles_power_workspace_size(int64_t n_particles, gbp_fft_plan plan,
                                        gbp_bins bins, int mas, int ells,
                                        size_t* bytes);
+/* Column tile shapes (tx x ty pencils, all of z) of the fused path for an
+ * n_mesh^3 mesh, the default first: up to `max` of them into tx[], ty[];
+ * *count = how many there are (no reference counterpart: the tile is the
+ * bucket of the particle sort, a tuning choice).  Every shape gives the same
+ * results bit for bit; they differ in speed, which the autotuner measures. */
+int gbp_column_tile_variants(int n_mesh, int* tx, int* ty, int max, int* count);
+/* Tile shape of a plan's fused calls: one of gbp_column_tile_variants, or
+ * 0, 0 for the default.  The workspace size depends on it: query after
+ * setting. */
+int gbp_fft_plan_set_tiles(gbp_fft_plan plan, int tx, int ty);
+/* The shape in effect (the default resolved). */
+int gbp_fft_plan_tiles(gbp_fft_plan plan, int* tx, int* ty);
 int gbp_particles_power(const float* x, const float* y, const float* z,
                         const float* w, int64_t n_particles, float xmin,
                         float ymin, float zmin, float inv_cell,
@@ -398,6 +411,9 @@ int gbp_deposit_backward(const float* x, const float* y, const float* z,
 typedef struct gbp_lane_s* gbp_lane;
 
 #define GBP_LANE_GRAPH 1   /* capture the launch sequence into a CUDA graph */
+/* Column tile of the lane's fused calls (gbp_fft_plan_set_tiles), or none
+ * for the default: flags |= GBP_LANE_TILES(tx, ty). */
+#define GBP_LANE_TILES(tx, ty) ((((tx) & 15) << 8) | (((ty) & 15) << 12))
 
 /* Per-job outputs (device pointers, any may be NULL), indexed by job j:
  * pk[(j*nb + b)*3 + l] (l = 0,2,4 -> 0,1,2), kmean[j*nb + b],

@@ -14,6 +14,7 @@ struct gbp_fft_plan_s {
   float2* tw;       // own transform: twiddles exp(-2 pi i e / N)
   int n, grids, pitch;
   size_t ws;
+  int tx = 0, ty = 0;   // column tile of the fused particles path (0: the default for n)
 };
 
 namespace gbp {

@@ -262,6 +262,10 @@ extern "C" int gbp_lane_create(int N, int mas, int interlace, int ells, int shot
   cudaGetDevice(&L->device);
   int st = gbp_fft_plan_create(N, L->G, &L->plan, &L->fft_ws);
   if (st) { lane_free(L); return st; }
+  if (flags & GBP_LANE_TILES(15, 15)) {
+    st = gbp_fft_plan_set_tiles(L->plan, (flags >> 8) & 15, (flags >> 12) & 15);
+    if (st) { lane_free(L); return st; }
+  }
   LaneSizes s{};
   s.fft = L->fft_ws;
   st = lane_sizes(N, mas, interlace, ells, bins, capacity, L->plan, s);

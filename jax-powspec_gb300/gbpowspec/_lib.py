@@ -69,6 +69,11 @@ JOB_BYTES = C.sizeof(Job)
 LANE_GRAPH = 1
 
 
+def lane_tiles_flag(tx: int, ty: int) -> int:
+    """GBP_LANE_TILES(tx, ty): the column tile a lane's fused calls use (0, 0: the default)."""
+    return ((int(tx) & 15) << 8) | ((int(ty) & 15) << 12)
+
+
 class TraceRecord(C.Structure):
     """Mirror of gbp_trace_record."""
 
@@ -112,6 +117,9 @@ SIGNATURES = [
     ("gbp_fft_power_workspace_size", _i, [_vp, _vp, _i, C.POINTER(_sz)]),
     ("gbp_fft_power", _i, [_vp, _vp, _vp, _vp, _i, _i, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     ("gbp_particles_power_workspace_size", _i, [_i64, _vp, _vp, _i, _i, C.POINTER(_sz)]),
+    ("gbp_column_tile_variants", _i, [_i, C.POINTER(_i), C.POINTER(_i), _i, C.POINTER(_i)]),
+    ("gbp_fft_plan_set_tiles", _i, [_vp, _i, _i]),
+    ("gbp_fft_plan_tiles", _i, [_vp, C.POINTER(_i), C.POINTER(_i)]),
     ("gbp_particles_power", _i, [_vp, _vp, _vp, _vp, _i64, _f, _f, _f, _f, _vp, _vp, _i, _i, _vp, _vp, _vp, _vp,
                                  _vp, _vp, _sz, _vp]),
     ("gbp_particles_power_job", _i, [_vp, _i64, _vp, _vp, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),

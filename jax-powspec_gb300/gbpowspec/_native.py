@@ -124,6 +124,16 @@ class FFTPlan:
     def spectrum_floats(self) -> int:
         return self.grids * self.n * self.n * self.pitch * 2
 
+    def set_tiles(self, tx: int = 0, ty: int = 0) -> None:
+        """Column tile (tx x ty pencils) of the fused particles path; 0, 0 = the default."""
+        check(_lib.load().gbp_fft_plan_set_tiles(self.handle, int(tx), int(ty)), "gbp_fft_plan_set_tiles")
+
+    @property
+    def tiles(self) -> tuple:
+        tx, ty = C.c_int(0), C.c_int(0)
+        check(_lib.load().gbp_fft_plan_tiles(self.handle, C.byref(tx), C.byref(ty)), "gbp_fft_plan_tiles")
+        return tx.value, ty.value
+
     def execute(self, mesh: torch.Tensor, spec: torch.Tensor, ws: torch.Tensor | None = None) -> torch.Tensor:
         n, G = self.n, self.grids
         if mesh.numel() != G * n ** 3 or mesh.dtype != _F32 or not mesh.is_contiguous():
@@ -140,6 +150,17 @@ class FFTPlan:
         if self.handle:
             _lib.load().gbp_fft_plan_destroy(self.handle)
             self.handle = None
+
+
+def tile_variants(n_mesh: int) -> list:
+    """Column tiles [(tx, ty), ...] of the fused path for an n_mesh^3 mesh, the default first ([] when the
+    mesh size has no fused path)."""
+    tx, ty, cnt = (C.c_int * 8)(), (C.c_int * 8)(), C.c_int(0)
+    st = _lib.load().gbp_column_tile_variants(int(n_mesh), tx, ty, 8, C.byref(cnt))
+    if st == _lib.GBP_ERR_UNSUPPORTED:
+        return []
+    check(st, "gbp_column_tile_variants")
+    return [(tx[i], ty[i]) for i in range(min(cnt.value, 8))]
 
 
 _plans: dict = {}

@@ -172,7 +172,7 @@ class BatchRunner:
 
     def __init__(self, n_mesh: int, *, capacity: int, mas: str = "cic", interlace: bool = True,
                  ells=(0, 2), kedges_grid=None, shot_noise: bool = True, kmean: bool = True,
-                 n_lanes: int = 2, graphs: bool = True, device=None):
+                 n_lanes: int = 2, graphs: bool = True, device=None, tiles="auto"):
         if not torch.cuda.is_available():
             raise RuntimeError("gbpowspec needs a CUDA device; there is no CPU fallback")
         self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
@@ -185,13 +185,21 @@ class BatchRunner:
         self.nb = self.bins.n_bins
         self.mask = _ells_mask(self.ells, self.kmean)
         lib = _lib.load()
+        # column tile of the lanes' fused calls: "auto" = the autotuner's choice for this shape (tune.py),
+        # None = the library default, or (tx, ty); the results are the same bits whatever the choice
+        if tiles == "auto":
+            from .tune import default_tuner
+            tiles = default_tuner().best(self.n_mesh, self.mas, self.interlace, n=self.capacity,
+                                         device=self.device) if _native.tile_variants(self.n_mesh) else None
+        self.tiles = None if tiles is None else (int(tiles[0]), int(tiles[1]))
+        flags = (_lib.LANE_GRAPH if graphs else 0) | (0 if self.tiles is None else _lib.lane_tiles_flag(*self.tiles))
         self._lanes = []
         with torch.cuda.device(self.device):
             for _ in range(int(n_lanes)):
                 h = C.c_void_p()
                 check(lib.gbp_lane_create(self.n_mesh, _lib.MAS[self.mas], int(self.interlace), self.mask,
-                                          int(self.shot_noise), self.bins.handle, self.capacity,
-                                          _lib.LANE_GRAPH if graphs else 0, C.byref(h)), "gbp_lane_create")
+                                          int(self.shot_noise), self.bins.handle, self.capacity, flags, C.byref(h)),
+                      "gbp_lane_create")
                 self._lanes.append(h)
         self._lane_arr = (C.c_void_p * len(self._lanes))(*[h.value for h in self._lanes])
         b = C.c_size_t(0)

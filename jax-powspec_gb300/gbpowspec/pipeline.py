@@ -111,7 +111,7 @@ class PowerSpectrum:
     cuFFT (gbp_fft_r2c) and bin it (gbp_power).
     """
 
-    def __init__(self, cfg: PkConfig, device=None):
+    def __init__(self, cfg: PkConfig, device=None, tiles=None):
         if not torch.cuda.is_available():
             raise RuntimeError("gbpowspec needs a CUDA device; there is no CPU fallback")
         self.cfg = cfg
@@ -119,7 +119,16 @@ class PowerSpectrum:
         N, G = cfg.n_mesh, cfg.grids
         dev = self.device
         self.stats = torch.empty(_lib.STATS_BYTES, dtype=torch.uint8, device=dev)
-        self.plan = _native.fft_plan(N, G, dev)
+        # column tile of the fused path: None = the library default, "auto" = the autotuner's choice for
+        # this shape (tune.py), or (tx, ty); every choice gives the same results bit for bit
+        if tiles == "auto":
+            from .tune import default_tuner
+            tiles = default_tuner().best(N, cfg.mas, cfg.interlace, device=dev)
+        if tiles is None or not _native.tile_variants(N):
+            self.plan = _native.fft_plan(N, G, dev)
+        else:
+            self.plan = _native.FFTPlan(N, G, dev)      # a plan of its own: the tile is a plan option
+            self.plan.set_tiles(*tiles)
         self.spec = torch.empty(self.plan.spectrum_floats, dtype=torch.float32, device=dev)
         self.bins = _native.bins_for(cfg.kedges_grid(), N, dev)
         self.ells = cfg.ells_mask()
@@ -140,6 +149,11 @@ class PowerSpectrum:
         edges = cfg.edges()
         self.k_edges = edges
         self.k_centres = torch.from_numpy(0.5 * (edges[1:].astype(np.float64) + edges[:-1])).to(dev)
+
+    @property
+    def tiles(self):
+        """The column tile (tx, ty) of the fused path, or None on the mesh path."""
+        return self.plan.tiles if self.fused else None
 
     def _ws(self, n: int) -> torch.Tensor:
         cfg = self.cfg

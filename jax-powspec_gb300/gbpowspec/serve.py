@@ -208,6 +208,9 @@ class Server:
         except Exception as e:                    # e.g. the device is out of memory: refuse, do not retry
             cls.failed = f"lane creation failed: {e}"
             return None
+        # the lane may hold a little more or less than the estimate (its tuned tile shape sizes the
+        # particle buckets): account what it holds
+        need = int(getattr(self.backend, "lane_bytes_of", lambda _lane: need)(lane))
         self.used += need
         slot = _Slot(lane, need)
         cls.slots.append(slot)
@@ -259,6 +262,9 @@ class GpuBackend:
 
     def create(self, req: Request, capacity: int):
         return _GpuLane(self, req, capacity)
+
+    def lane_bytes_of(self, lane) -> int:
+        return lane.runner.device_bytes + lane.xyz.numel() * 4 + 4096
 
     def destroy(self, lane):
         lane.close()
