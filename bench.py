@@ -640,14 +640,18 @@ def main():
         dist.destroy_process_group()
 
 
-# DRAM bytes (read + write) per launch from ncu captures of the same kernels
-# (--set full, --clock-control none), keyed by (kernel, mesh, particles).  The
-# x pass + binning reads only the spectra, so its traffic does not depend on
-# the particle count: the 512^3 figure comes from a capture with 1,048,576
-# particles and serves the 4,194,304-particle workload unchanged.
+# DRAM bytes (read + write) per launch from one ncu capture of the same kernels
+# (--set full, --clock-control none) on 512^3 with 1,048,576 particles,
+# keyed by (kernel, mesh, particles).  The y pass and the x pass + binning
+# move only spectra, so their traffic does not depend on the particle count.
+# The deposit/z kernel writes the z-transformed spectra (1.048 GB, particle
+# independent) and reads its bucket entries (0.037 GB at 1,048,576
+# particles, in proportion to the particles): 1.048 + 4 x 0.037 GB for the
+# 4,194,304-particle workload.
 PROFILED_TRAFFIC = {
-    ("deposit_tiles", 512, 4_194_304): 1_123_164_000,
-    ("fft_x_bins", 512, 4_194_304): 1_114_337_000,
+    ("deposit_fft_z", 512, 4_194_304): 1_048_093_000 + 4 * 37_086_000,
+    ("fft_y", 512, 4_194_304): 1_107_356_000 + 1_053_230_000,
+    ("fft_x_bins", 512, 4_194_304): 1_107_791_000 + 6_489_000,
 }
 
 
