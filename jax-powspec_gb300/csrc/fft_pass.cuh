@@ -175,13 +175,17 @@ struct ColBlock {
   __device__ static __forceinline__ int at(int j, int cp) { return (cp >> 2) * (SLAB / 2) + row(j) * 4 + (cp & 3); }
 };
 
-template <int N, int SLABS, int NT, bool OUT_SHARED, class In, class Out>
+// IN_SHARED: the first stage's shared-memory writes must wait for earlier
+// readers of `s` (a barrier between its loads and its writes), so a caller
+// can start the loads of the next block while other warps still read the
+// previous one.
+template <int N, int SLABS, int NT, bool OUT_SHARED, class In, class Out, bool IN_SHARED = false>
 __device__ __forceinline__ void col_fft(float2* s, In gin, Out gout, const float2* __restrict__ tw, int tid) {
   using L = ColBlock<N, SLABS>;
   float4* s4 = reinterpret_cast<float4*>(s);
   auto sin_ = [s4](int j, int cp) { return s4[L::at(j, cp)]; };
   auto sout = [s4](int j, int cp, float4 v) { s4[L::at(j, cp)] = v; };
-  run_stages2<N, L::CP, NT, false, false, OUT_SHARED>(gin, sin_, sout, gout, tw, tid);
+  run_stages2<N, L::CP, NT, false, IN_SHARED, OUT_SHARED>(gin, sin_, sout, gout, tw, tid);
 }
 
 // Slot of row j in a column-major block of column pairs (IFAST stages).

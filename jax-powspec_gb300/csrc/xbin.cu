@@ -12,10 +12,13 @@
 //      Stockham stages (fft_core.cuh); the last stage writes the result
 //      column-major with an XOR swizzle, so the binning reads it without
 //      bank conflicts,
-//   3. bins the 8 x N modes: a warp walks one column over half of the x
-//      axis, where |kx| is monotone (x = 0..N/2-1: kx = 0..N/2-1; x =
-//      N/2..N-1: |kx| = N/2..1), so bins are monotone along the walk.  A lane
-//      owns consecutive modes; runs of equal bin are summed in-lane, joined
+//   3. bins the 8 x N modes: from 128^3 up the modes x and N - x of a
+//      column (kx and -kx) share |k|, mu, the window and the bin, so they
+//      are summed first and looked up once; a warp walks one column over
+//      half of the |kx| range (pairs p = 0..N/4-1 or N/4..N/2-1; x = N/2
+//      alone is added after the upper half), so bins are monotone along the
+//      walk (at 64^3: single modes over half of the x axis).  A lane owns
+//      consecutive pairs; runs of equal bin are summed in-lane, joined
 //      across lanes by one warp segmented scan, and each run is added once
 //      to the warp's float32 bins (distinct bins within a step: no atomics).
 //
@@ -42,12 +45,20 @@ namespace {
 constexpr int XB_THREADS = 512;
 constexpr int XB_BINS = 8;                   // per-warp bin arrays; warps w and w + 8 share one
 constexpr int XB_C = 8;                      // kz columns per work item
+// The next item's HBM loads start before the barrier that ends the binning (512^3 and up)
+template <int N>
+constexpr bool XB_EARLY = N >= 512;
 
 template <int N>
 struct XLayout {
   static constexpr int TST = N + 1;          // complex per column (transposed layout); odd: no store conflicts
   static constexpr int M = N / 64;           // modes per lane in a half axis
   static constexpr int MS = M < 8 ? M : 8;   // modes per lane and warp step
+  // N >= 128: the modes x and N - x of a column (kx and -kx: the same |k|, mu, window and bin) are
+  // binned together, M2 such pairs per lane in half of the |kx| range
+  static constexpr bool PAIRED = N >= 128;
+  static constexpr int M2 = N / 128;
+  static constexpr int MS2 = M2 < 8 ? M2 : 8;
   static __host__ __device__ constexpr size_t data_bytes(int G) {
     const size_t rows = (size_t)G * fft::ColBlock<N, 2>::SLAB, cols = (size_t)G * XB_C * TST;
     return ((rows > cols ? rows : cols) * 8 + 127) & ~size_t(127);
@@ -56,16 +67,17 @@ struct XLayout {
   static __host__ __device__ constexpr size_t xtab_bytes() { return (size_t)N * 12; }
 };
 
-// Swizzled position of x in a transposed column: a lane's consecutive modes
-// sit 16-apart in bank slots, so the 16 lanes of a half-warp hit 16 slots.
+// Swizzled position of x in a transposed column: lane l reads x = base + L l
+// (L = the modes or mode pairs a lane takes per half axis), and so does it
+// read the mirror N - x; with x's low bits XORed by bits 4.. of x, the 16
+// lanes of a half-warp hit 16 distinct 8-byte slots in both reads, and the
+// last FFT stage's stores stay conflict-free (checked by enumeration of
+// every stage and mesh size).
 template <int N>
 __device__ __forceinline__ int xswz(int x) {
-  constexpr int M = XLayout<N>::M;
-  if constexpr (M == 1) return x;
-  else if constexpr (M == 2) return x ^ ((x >> 4) & 1);
-  else if constexpr (M == 4) return x ^ ((x >> 4) & 3);
-  else if constexpr (M == 8) return x ^ ((x >> 4) & 7);
-  else return x ^ ((x >> 4) & 15);
+  constexpr int L = XLayout<N>::PAIRED ? XLayout<N>::M2 : XLayout<N>::M;
+  if constexpr (L <= 1) return x;
+  else return x ^ ((x >> 4) & (L - 1));
 }
 
 // One warp step: lane modes x0 + j (j < MS) of one column, bins monotone in
@@ -146,9 +158,64 @@ __device__ __forceinline__ void xbin_modes(const PowGeom& g, const Smem& t, cons
   }
 }
 
+// Moments and bins of one warp step of mode pairs: lane pairs p0 .. p0 + MS - 1
+// of column (a_col, b_col), pair p = the columns x = p and x = N - p
+// (kx = p and -p), whose |k|, mu, window and bin agree; p = 0 is x = 0 alone.
+template <int N, int NV, bool INTER, int MS>
+__device__ __forceinline__ void xbin_pairs(const PowGeom& g, const Smem& t, const float* c2x, const float2* ephx,
+                                           const float2* a_col, const float2* b_col, int p0, int kyz2, float cyz,
+                                           float fz2, float2 eyz, float (&P)[MS][NV], int (&bin)[MS]) {
+#pragma unroll
+  for (int j = 0; j < MS; ++j) {
+    const int p = p0 + j;
+    const int sp = xswz<N>(p), sm = xswz<N>((N - p) & (N - 1));
+    const float2 a = a_col[sp], am = a_col[sm];
+    float re = a.x, im = a.y, rem = am.x, imm = am.y;
+    if (INTER) {
+      const float2 b = b_col[sp], bm = b_col[sm];
+      const float2 ex = ephx[sp];                            // exp(i pi p / N); kx = -p takes its conjugate
+      const float ar = ex.x * eyz.x, ai = ex.x * eyz.y, br = ex.y * eyz.y, bi = ex.y * eyz.x;
+      const float qr = ar - br, qi = ai + bi;                // exp(i pi p / N) eyz
+      const float mr = ar + br, mi = ai - bi;                // exp(-i pi p / N) eyz
+      re = a.x + (b.x * qr - b.y * qi);
+      im = a.y + (b.x * qi + b.y * qr);
+      rem = am.x + (bm.x * mr - bm.y * mi);
+      imm = am.y + (bm.x * mi + bm.y * mr);
+    }
+    const int k2 = p * p + kyz2;
+    float pw = re * re + im * im;
+    if (g.zero_dc && k2 == 0) pw = 0.0f;
+    if (p > 0) pw += rem * rem + imm * imm;
+    const float v = pw * (cyz * c2x[sp]);
+    P[j][0] = v;
+    if (NV > 1) {
+      const float mu2 = k2 > 0 ? __fdividef(fz2, (float)k2) : 0.0f;
+      P[j][1] = v * mu2;
+      if (NV > 2) P[j][2] = P[j][1] * mu2;
+    }
+    bin[j] = bin_of(g, t, k2);
+  }
+}
+
+// The column x = N/2 (kx = N/2, its own mirror) of one column, added to the
+// warp's bins by one lane.  Out of line: it runs once per column and only
+// for bins beyond k_Nyq, and inlined it would cost the binning registers.
+template <int N, int NV, bool INTER>
+__device__ __noinline__ void add_nyquist_x(const PowGeom& g, const Smem& t, const float* c2x, const float2* ephx,
+                                           const float2* a_col, const float2* b_col, int kyz2, float cyz, float fz2,
+                                           float2 eyz, float* wb) {
+  float P[1][NV];
+  int bin[1];
+  xbin_modes<N, NV, INTER, 1>(g, t, c2x, ephx, a_col, b_col, N / 2, kyz2, cyz, fz2, eyz, P, bin);
+  if (bin[0] >= 0) bin_add<NV>(wb, g.nbe, bin[0], P[0]);
+}
+
 // Bin the 8 columns of one item (transposed layout in s).  Warp w takes
-// column w / 2 and half w % 2 of the x axis; warps w and w + 8 share bin
-// array w % 8 and flush in two phases separated by barriers.
+// column w / 2 and half w % 2 of the x axis (of the |kx| range, in mode
+// pairs x, N - x from 128^3 up); warps w and w + 8 share bin
+// array w % 8 and flush in two phases separated by barriers.  No barrier
+// follows the last step: the caller's next barrier (the next item's first
+// FFT stage, or the fold) orders the last flushes and reads of s.
 template <int N, int NV, bool INTER>
 __device__ __forceinline__ void xbin_item(const PowGeom& g, const Smem& t, const float* c2x, const float2* ephx,
                                           const float2* s, int warp, int lane, int y, int kb) {
@@ -173,25 +240,44 @@ __device__ __forceinline__ void xbin_item(const PowGeom& g, const Smem& t, const
   const float2* a_col = s + c * TST;
   const float2* b_col = s + (XB_C + c) * TST;
   float* wb = t.wbase + (warp & (XB_BINS - 1)) * NV * g.nbe;
+  if constexpr (XLayout<N>::PAIRED) {
+    // warp half h walks pairs h N/4 .. (h+1) N/4 - 1 (|kx| ascending); the column x = N/2, its own
+    // mirror, is added by lane 0 of the upper half after its last flush
+    constexpr int M2 = XLayout<N>::M2, MS2 = XLayout<N>::MS2;
 #pragma unroll 1
-  for (int s0 = 0; s0 < M; s0 += MS) {
-    float P[MS][NV];
-    int bin[MS];
-    if (active) {
-      xbin_modes<N, NV, INTER, MS>(g, t, c2x, ephx, a_col, b_col, h * H + lane * M + s0, kyz2, cyz, fz2, eyz, P,
-                                   bin);
-    } else {
-#pragma unroll
-      for (int j = 0; j < MS; ++j) {
-        bin[j] = -1;
-#pragma unroll
-        for (int q = 0; q < NV; ++q) P[j][q] = 0.0f;
-      }
+    for (int s0 = 0; s0 < M2; s0 += MS2) {
+      float P[MS2][NV];
+      int bin[MS2];
+      if (active)
+        xbin_pairs<N, NV, INTER, MS2>(g, t, c2x, ephx, a_col, b_col, h * (H / 2) + lane * M2 + s0, kyz2, cyz, fz2,
+                                      eyz, P, bin);
+      auto flush = [&]() {
+        flush_runs<MS2, NV>(P, bin, lane, wb, g.nbe);
+        // |kx| = N/2 reaches a bin only when the last edge lies beyond k_Nyq
+        if (h == 1 && s0 + MS2 >= M2 && (H * H + kyz2 <= g.tu)) {
+          if (lane == 0) add_nyquist_x<N, NV, INTER>(g, t, c2x, ephx, a_col, b_col, kyz2, cyz, fz2, eyz, wb);
+          __syncwarp();
+        }
+      };
+      if (warp < XB_BINS && active) flush();
+      __syncthreads();
+      if (warp >= XB_BINS && active) flush();
+      if (s0 + MS2 < M2) __syncthreads();   // after the last step, the next item's (or the fold's) barrier follows
     }
-    if (warp < XB_BINS && active) flush_runs<MS, NV>(P, bin, lane, wb, g.nbe);
-    __syncthreads();
-    if (warp >= XB_BINS && active) flush_runs<MS, NV>(P, bin, lane, wb, g.nbe);
-    __syncthreads();
+  } else {
+#pragma unroll 1
+    for (int s0 = 0; s0 < M; s0 += MS) {
+      float P[MS][NV];
+      int bin[MS];
+      if (active) {
+        xbin_modes<N, NV, INTER, MS>(g, t, c2x, ephx, a_col, b_col, h * H + lane * M + s0, kyz2, cyz, fz2, eyz, P,
+                                     bin);
+      }
+      if (warp < XB_BINS && active) flush_runs<MS, NV>(P, bin, lane, wb, g.nbe);
+      __syncthreads();
+      if (warp >= XB_BINS && active) flush_runs<MS, NV>(P, bin, lane, wb, g.nbe);
+      if (s0 + MS < M) __syncthreads();     // after the last step, the next item's (or the fold's) barrier follows
+    }
   }
 }
 
@@ -227,8 +313,12 @@ xbin_kernel(PowGeom g) {
         s[(2 * cp) * TST + xswz<N>(x)] = fft::lo2(v);
         s[(2 * cp + 1) * TST + xswz<N>(x)] = fft::hi2(v);
       };
-      fft::col_fft<N, G, XB_THREADS, true>(s, gin, tout, g.tw, tid);   // ends with a barrier
-      xbin_item<N, NV, INTER>(g, t, c2x, ephx, s, warp, lane, y, kb);  // ends with a barrier
+      // from 512^3 up the first stage loads the item from HBM while the previous item's last warps
+      // still bin it, and waits for them before it writes the shared buffer (smaller meshes: the
+      // registers the early loads hold would spill; they end the binning with a barrier instead)
+      fft::col_fft<N, G, XB_THREADS, true, decltype(gin), decltype(tout), XB_EARLY<N>>(s, gin, tout, g.tw, tid);
+      xbin_item<N, NV, INTER>(g, t, c2x, ephx, s, warp, lane, y, kb);
+      if constexpr (!XB_EARLY<N>) __syncthreads();
     }
     cta_fold<NV>(g, t, grp);
   }
