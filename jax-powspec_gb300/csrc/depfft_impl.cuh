@@ -251,47 +251,59 @@ __device__ __forceinline__ bool block_scales(const DepGeom& g, const float4* __r
                                              unsigned end, int x0, int y0, int* zc, int* s_max, int (&sh)[CT::NSB]) {
   constexpr int R = MAS, NT = CT::NT, NSB = CT::NSB, W = R + G - 1;
   const int tid = threadIdx.x;
-  for (unsigned i = beg + tid; i < end; i += NT) {
-    const float4 e = entries[i];
-    // the union of the grids' nodes along each axis: first .. last (the second grid's first node
-    // is the first grid's or the next one), as the bucketing counts them.  Every entry of the
-    // bucket reaches the tile, so an axis with one block row needs no test
-    int first[3], last[3];
+  // this pass is the tile's first touch of its bucket: a thread issues EB entry loads at once
+  constexpr int EB = 4;
+  for (unsigned i0 = beg + tid; i0 < end; i0 += EB * NT) {
+    float4 ev[EB];
 #pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      if ((a == 0 && CT::SBX == 1) || (a == 1 && CT::SBY == 1)) {
-        first[a] = last[a] = 0;
-        continue;
-      }
-      Axis<R> a0;
-      make_axis<MAS, 0>(g, a == 0 ? e.x : (a == 1 ? e.y : e.z), 0, a0);
-      first[a] = a0.first;
-      last[a] = a0.first + R - 1;
-      if constexpr (G == 2) {
-        Axis<R> a1;
-        make_axis<MAS, 0>(g, a == 0 ? e.x : (a == 1 ? e.y : e.z), 1, a1);
-        last[a] = a1.first + R - 1;
-      }
-    }
-    // scale blocks reached along x and y
-    unsigned mx = CT::SBX == 1 ? 1u : 0u, my = CT::SBY == 1 ? 1u : 0u;
-#pragma unroll
-    for (int r = 0; r < W; ++r) {
-      if constexpr (CT::SBX > 1) {
-        const int cx = wrapn(first[0] + r, N) - x0;
-        if (first[0] + r <= last[0] && cx >= 0 && cx < CT::TX) mx |= 1u << (cx >> 2);
-      }
-      if constexpr (CT::SBY > 1) {
-        const int cy = wrapn(first[1] + r, N) - y0;
-        if (first[1] + r <= last[1] && cy >= 0 && cy < CT::TY) my |= 1u << (cy >> 2);
-      }
+    for (int k = 0; k < EB; ++k) {
+      const unsigned i = i0 + k * NT;
+      ev[k] = i < end ? entries[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     }
 #pragma unroll
-    for (int bx = 0; bx < CT::SBX; ++bx)
+    for (int k = 0; k < EB; ++k) {
+      if (i0 + k * NT >= end) break;
+      const float4 e = ev[k];
+      // the union of the grids' nodes along each axis: first .. last (the second grid's first node
+      // is the first grid's or the next one), as the bucketing counts them.  Every entry of the
+      // bucket reaches the tile, so an axis with one block row needs no test
+      int first[3], last[3];
 #pragma unroll
-      for (int by = 0; by < CT::SBY; ++by)
-        if (((mx >> bx) & 1u) && ((my >> by) & 1u))
-          for (int zn = first[2]; zn <= last[2]; ++zn) atomicAdd(&zc[(bx * CT::SBY + by) * N + wrapn(zn, N)], 1);
+      for (int a = 0; a < 3; ++a) {
+        if ((a == 0 && CT::SBX == 1) || (a == 1 && CT::SBY == 1)) {
+          first[a] = last[a] = 0;
+          continue;
+        }
+        Axis<R> a0;
+        make_axis<MAS, 0>(g, a == 0 ? e.x : (a == 1 ? e.y : e.z), 0, a0);
+        first[a] = a0.first;
+        last[a] = a0.first + R - 1;
+        if constexpr (G == 2) {
+          Axis<R> a1;
+          make_axis<MAS, 0>(g, a == 0 ? e.x : (a == 1 ? e.y : e.z), 1, a1);
+          last[a] = a1.first + R - 1;
+        }
+      }
+      // scale blocks reached along x and y
+      unsigned mx = CT::SBX == 1 ? 1u : 0u, my = CT::SBY == 1 ? 1u : 0u;
+#pragma unroll
+      for (int r = 0; r < W; ++r) {
+        if constexpr (CT::SBX > 1) {
+          const int cx = wrapn(first[0] + r, N) - x0;
+          if (first[0] + r <= last[0] && cx >= 0 && cx < CT::TX) mx |= 1u << (cx >> 2);
+        }
+        if constexpr (CT::SBY > 1) {
+          const int cy = wrapn(first[1] + r, N) - y0;
+          if (first[1] + r <= last[1] && cy >= 0 && cy < CT::TY) my |= 1u << (cy >> 2);
+        }
+      }
+#pragma unroll
+      for (int bx = 0; bx < CT::SBX; ++bx)
+#pragma unroll
+        for (int by = 0; by < CT::SBY; ++by)
+          if (((mx >> bx) & 1u) && ((my >> by) & 1u))
+            for (int zn = first[2]; zn <= last[2]; ++zn) atomicAdd(&zc[(bx * CT::SBY + by) * N + wrapn(zn, N)], 1);
+    }
   }
   __syncthreads();
   // a node weight of TSC (<= 0.75^3) or PCS (<= (2/3)^3) is below 1/2: one more bit
