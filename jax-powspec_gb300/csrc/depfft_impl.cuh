@@ -210,25 +210,33 @@ __device__ __forceinline__ long long tile_grid(const DepGeom& g, const float4* _
     }
   }
 
-  // split the packed spectra; write all pencils' rows (row padding -> 0)
+  // split the packed spectra; write all pencils' rows (row padding -> 0), two k per thread and
+  // 16-byte stores
   const float2* cs = reinterpret_cast<const float2*>(cs4);
   float2* out = spec + grid * gstride;
-  for (int idx = tid; idx < PAIRS * P; idx += NT) {
-    const int q = idx / P, k = idx - (idx / P) * P;
-    float2 a = make_float2(0.f, 0.f), b = make_float2(0.f, 0.f);
-    if (k <= H) {
-      const float2 c = cs[((q >> 1) * N + fft::zsw(k)) * 2 + (q & 1)];
-      const float2 m = cs[((q >> 1) * N + fft::zsw((N - k) & (N - 1))) * 2 + (q & 1)];
-      const float2 cm = make_float2(m.x, -m.y);
-      const float2 sum = fft::cadd(c, cm), dif = fft::cmi(fft::csub(c, cm));
-      a = make_float2(0.5f * sum.x, 0.5f * sum.y);
-      b = make_float2(0.5f * dif.x, 0.5f * dif.y);
+  constexpr int P2 = P / 2;
+  for (int idx = tid; idx < PAIRS * P2; idx += NT) {
+    const int q = idx / P2, k0 = 2 * (idx - q * P2);
+    const float2* col = cs + (q >> 1) * N * 2 + (q & 1);
+    float2 a[2], b[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int k = k0 + h;
+      a[h] = b[h] = make_float2(0.f, 0.f);
+      if (k <= H) {
+        const float2 c = col[fft::zsw(k) * 2];
+        const float2 m = col[fft::zsw((N - k) & (N - 1)) * 2];
+        const float2 cm = make_float2(m.x, -m.y);
+        const float2 sum = fft::cadd(c, cm), dif = fft::cmi(fft::csub(c, cm));
+        a[h] = make_float2(0.5f * sum.x, 0.5f * sum.y);
+        b[h] = make_float2(0.5f * dif.x, 0.5f * dif.y);
+      }
     }
     const int f0 = 2 * q, f1 = 2 * q + 1;
     const long long r0 = (long long)(x0 + f0 / TY) * N + (y0 + f0 % TY);
     const long long r1 = (long long)(x0 + f1 / TY) * N + (y0 + f1 % TY);
-    __stcs(out + r0 * P + k, a);
-    __stcs(out + r1 * P + k, b);
+    __stcs(reinterpret_cast<float4*>(out + r0 * P + k0), make_float4(a[0].x, a[0].y, a[1].x, a[1].y));
+    __stcs(reinterpret_cast<float4*>(out + r1 * P + k0), make_float4(b[0].x, b[0].y, b[1].x, b[1].y));
   }
 
   // the tile's exact total

@@ -68,22 +68,32 @@ fftz_kernel(const float* __restrict__ mesh, float2* __restrict__ out, long long 
   auto sout = [](int j, int cp, float4 v) { s4[cp * N + zsw(j)] = v; };
   fft::run_stages2<N, CP, NT, true, false, true>(gin, sin_, sout, sout, tw, tid);
 
-  // split the packed spectra and write both pencils' rows (padding -> 0)
+  // split the packed spectra and write both pencils' rows (padding -> 0); two k per thread and
+  // 16-byte stores (rows are P = N/2 + 8 complex: 16-byte aligned)
   const float2* s2 = reinterpret_cast<const float2*>(s4);
-  for (int idx = tid; idx < PAIRS * P; idx += NT) {
-    const int q = idx / P, k = idx - (idx / P) * P;
+  constexpr int P2 = P / 2;
+  for (int idx = tid; idx < PAIRS * P2; idx += NT) {
+    const int q = idx / P2, k0 = 2 * (idx - q * P2);
     if (2 * q >= npen) continue;
-    float2 a = make_float2(0.f, 0.f), b = make_float2(0.f, 0.f);
-    if (k <= H) {
-      const float2 c = s2[((q >> 1) * N + zsw(k)) * 2 + (q & 1)];
-      const float2 m = s2[((q >> 1) * N + zsw((N - k) & (N - 1))) * 2 + (q & 1)];
-      const float2 cm = make_float2(m.x, -m.y);
-      const float2 sum = cadd(c, cm), dif = cmi(csub(c, cm));
-      a = make_float2(0.5f * sum.x, 0.5f * sum.y);
-      b = make_float2(0.5f * dif.x, 0.5f * dif.y);
+    const float2* col = s2 + (q >> 1) * N * 2 + (q & 1);
+    float2 a[2], b[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int k = k0 + h;
+      a[h] = b[h] = make_float2(0.f, 0.f);
+      if (k <= H) {
+        const float2 c = col[zsw(k) * 2];
+        const float2 m = col[zsw((N - k) & (N - 1)) * 2];
+        const float2 cm = make_float2(m.x, -m.y);
+        const float2 sum = cadd(c, cm), dif = cmi(csub(c, cm));
+        a[h] = make_float2(0.5f * sum.x, 0.5f * sum.y);
+        b[h] = make_float2(0.5f * dif.x, 0.5f * dif.y);
+      }
     }
-    __stcs(out + (pen0 + 2 * q) * P + k, a);
-    if (2 * q + 1 < npen) __stcs(out + (pen0 + 2 * q + 1) * P + k, b);
+    __stcs(reinterpret_cast<float4*>(out + (pen0 + 2 * q) * P + k0), make_float4(a[0].x, a[0].y, a[1].x, a[1].y));
+    if (2 * q + 1 < npen)
+      __stcs(reinterpret_cast<float4*>(out + (pen0 + 2 * q + 1) * P + k0),
+             make_float4(b[0].x, b[0].y, b[1].x, b[1].y));
   }
 }
 
