@@ -291,7 +291,7 @@ def covariance_leg(dev, seed: int, n_mocks: int = 256) -> dict:
     return out
 
 
-def serving_leg(dev, seed: int, seconds: float = 10.0, rate: float = 200.0) -> dict:
+def serving_leg(dev, seed: int, seconds: float = 10.0, rate: float = 200.0, lanes: int = 2) -> dict:
     """Serving stream: Poisson arrivals (mean `rate`/s) for `seconds`; mesh 128/256/512 w.p. 0.5/0.35/0.15,
     particle counts log-uniform [1e5, 1e7], MAS CIC or TSC, L from U[500, 2500]; 80 GB budget.
     Client data: a pool of 8 device-generated lognormal catalogues of 1e7 particles (one box each, drawn from
@@ -315,12 +315,12 @@ def serving_leg(dev, seed: int, seconds: float = 10.0, rate: float = 200.0) -> d
         N = int(rng.choice([128, 256, 512], p=[0.5, 0.35, 0.15]))
         mas = str(rng.choice(["cic", "tsc"]))
         reqs.append(Request(x[:n], y[:n], z[:n], box=box, n_mesh=N, mas=mas))
-    srv = Server(budget_bytes=80e9, lanes_per_class=2, capacity=10_000_000, device=dev)
+    srv = Server(budget_bytes=80e9, lanes_per_class=lanes, capacity=10_000_000, device=dev)
     # warm every class once (lane creation and graph capture are not part of the stream)
     for N in (128, 256, 512):
         for mas in ("cic", "tsc"):
             box, (x, y, z) = pool[0]
-            for _ in range(2):                                   # both lanes of the class
+            for _ in range(lanes):                               # every lane of the class
                 srv.submit(Request(x[:1000], y[:1000], z[:1000], box=box, n_mesh=N, mas=mas))
     srv.drain(timeout=300)
     results = []
@@ -350,7 +350,7 @@ def serving_leg(dev, seed: int, seconds: float = 10.0, rate: float = 200.0) -> d
             "p99_ms": None if p["p99"] is None else p["p99"] * 1e3,
             "per_mesh": per_class,
             "throughput_rps": len(ok) / t_end, "particles_per_s": sum(r.n_kept for r in ok) / t_end,
-            "lanes_per_class": 2, "stream_priority": "128^3 lanes highest, 512^3 lowest",
+            "lanes_per_class": lanes, "stream_priority": "128^3 lanes highest, 512^3 lowest",
             "resident_lanes_gb": resident / 1e9}
 
 
@@ -457,6 +457,7 @@ def main():
     ap.add_argument("--no-serve", action="store_true", help="skip the serving leg")
     ap.add_argument("--no-extensions", action="store_true", help="skip the xi / bispectrum / gradient timings")
     ap.add_argument("--serve-seconds", type=float, default=10.0)
+    ap.add_argument("--serve-lanes", type=int, default=2, help="resident lanes per request class")
     ap.add_argument("--profile-only", action="store_true",
                     help="plain path only, warm-up + timed steps (no other legs): a short command for ncu")
     args = ap.parse_args()
@@ -572,7 +573,7 @@ def main():
     if not args.no_covariance:
         extra["batched_covariance"] = covariance_leg(dev, seed=3000 + rank)
     if not args.no_serve:
-        extra["serving"] = serving_leg(dev, seed=4000 + rank, seconds=args.serve_seconds)
+        extra["serving"] = serving_leg(dev, seed=4000 + rank, seconds=args.serve_seconds, lanes=args.serve_lanes)
     if not args.no_extensions:
         extra["extensions"] = extensions_leg(dev, seed=5000 + rank)
 

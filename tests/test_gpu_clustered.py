@@ -74,3 +74,34 @@ def test_clustered_catalogue_against_fp64(case, mas, interlace):
     for l in range(3):
         err = np.abs(pk[full, l] - ref["pk"][full, l]) / amp
         assert err.max() <= 1e-5, (l, float(err.max()))
+
+
+@pytest.mark.parametrize("mas", ["cic", "tsc"])
+def test_dense_mesh_every_tile_takes_the_64bit_path(mas):
+    """8,388,608 uniform particles on a 64^3 mesh: thousands of entries cover every plane of every
+    block, so every tile goes through the 64-bit kernel (many tiles per CTA); against float64, and
+    the same bits for every tile shape."""
+    import fp64_torch as F
+    from gbpowspec import PkConfig, PowerSpectrum, _native, read_stats
+    from gbpowspec.batch import shell_edges
+    N, box, n = 64, 500.0, 1 << 23
+    g = torch.Generator(device="cuda").manual_seed(9)
+    x, y, z = (torch.rand(n, generator=g, device="cuda") * box for _ in range(3))
+    order = {"cic": 2, "tsc": 3}[mas]
+    cfg = PkConfig(n_mesh=N, box_size=box, mas=mas, interlace=True, k_edges_kf=tuple(shell_edges(N).tolist()))
+    outs = []
+    for tiles in _native.tile_variants(N):
+        r = PowerSpectrum(cfg, tiles=tiles).run(x, y, z)
+        torch.cuda.synchronize()
+        outs.append((r.pk.clone(), r.stats.clone()))
+    for pk, st in outs[1:]:
+        assert torch.equal(st, outs[0][1])
+        assert torch.equal(torch.nan_to_num(pk, nan=-7.0), torch.nan_to_num(outs[0][0], nan=-7.0))
+    ref = F.power_multipoles(x, y, z, box=box, N=N, mas=order, interlace=True, kedges_grid=shell_edges(N))
+    np.testing.assert_allclose(read_stats(outs[0][1]).mass[0], ref["mass"], rtol=1e-6)
+    pk = outs[0][0].cpu().numpy()
+    full = ref["nmodes"] > 0
+    amp = np.abs(ref["pk"][full, 0] + ref["shot"]) + ref["shot"]
+    for l in range(3):
+        err = np.abs(pk[full, l] - ref["pk"][full, l]) / amp
+        assert err.max() <= 1e-5, (l, float(err.max()))
