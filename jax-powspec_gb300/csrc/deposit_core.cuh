@@ -303,7 +303,7 @@ count_kernel(DepGeom gp, unsigned* __restrict__ counts, DepCounters* ctr, float4
 
 // Pass 3: append (u_x, u_y, u_z, w) to every touched tile's bucket.
 template <int MAS, int G, int CM>
-__global__ void __launch_bounds__(CNT_THREADS)
+__global__ void __launch_bounds__(CNT_THREADS, 4)
 scatter_kernel(DepGeom gp, const unsigned* __restrict__ offsets, unsigned* __restrict__ fills,
                float4* __restrict__ entries) {
   DepGeom g = gp;
@@ -322,12 +322,34 @@ scatter_kernel(DepGeom gp, const unsigned* __restrict__ offsets, unsigned* __res
     const int nz = axis_tiles<MAS, G, CM>(g, 2, u[2], z0, z1, z2);
     if (nx * ny * nz == 0) continue;
     const float4 e = make_float4(u[0], u[1], u[2], w);
-    for (int a = 0; a < nx; ++a)
-      for (int b = 0; b < ny; ++b)
-        for (int c = 0; c < nz; ++c) {
-          const int t = (pick3(a, x0, x1, x2) * g.nt[1] + pick3(b, y0, y1, y2)) * g.nt[2] + pick3(c, z0, z1, z2);
-          entries[offsets[t] + atomicAdd(&fills[t * CSTRIDE], 1u)] = e;
+    if (nx <= 2 && ny <= 2 && nz <= 2) {
+      // at most 2 x 2 x 2 tiles (every tile at least as wide as the stencil): all slots claimed at
+      // once, so the returning atomics of one particle overlap instead of forming a chain
+      int tt[8];
+      unsigned base[8], slot[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int a = q >> 2, b = (q >> 1) & 1, c = q & 1;
+        tt[q] = (a < nx && b < ny && c < nz)
+                    ? ((a ? x1 : x0) * g.nt[1] + (b ? y1 : y0)) * g.nt[2] + (c ? z1 : z0) : -1;
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        if (tt[q] >= 0) {
+          base[q] = offsets[tt[q]];
+          slot[q] = atomicAdd(&fills[tt[q] * CSTRIDE], 1u);
         }
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        if (tt[q] >= 0) entries[base[q] + slot[q]] = e;
+    } else {
+      for (int a = 0; a < nx; ++a)
+        for (int b = 0; b < ny; ++b)
+          for (int c = 0; c < nz; ++c) {
+            const int t = (pick3(a, x0, x1, x2) * g.nt[1] + pick3(b, y0, y1, y2)) * g.nt[2] + pick3(c, z0, z1, z2);
+            entries[offsets[t] + atomicAdd(&fills[t * CSTRIDE], 1u)] = e;
+          }
+    }
   }
 }
 
