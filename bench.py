@@ -647,12 +647,12 @@ def main():
 # move only spectra, so their traffic does not depend on the particle count.
 # The deposit/z kernel writes the z-transformed spectra (1.048 GB, particle
 # independent) and reads its bucket entries (0.037 GB at 1,048,576
-# particles, in proportion to the particles): 1.048 + 4 x 0.037 GB for the
+# particles, in proportion to the particles): 1.047 + 4 x 0.037 GB for the
 # 4,194,304-particle workload.
 PROFILED_TRAFFIC = {
-    ("deposit_fft_z", 512, 4_194_304): 1_048_093_000 + 4 * 37_086_000,
-    ("fft_y", 512, 4_194_304): 1_107_356_000 + 1_053_230_000,
-    ("fft_x_bins", 512, 4_194_304): 1_107_791_000 + 6_489_000,
+    ("deposit_fft_z", 512, 4_194_304): 1_046_606_000 + 4 * 37_221_000,
+    ("fft_y", 512, 4_194_304): 1_107_357_000 + 1_053_285_000,
+    ("fft_x_bins", 512, 4_194_304): 1_107_393_000 + 6_821_000,
 }
 
 
