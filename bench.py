@@ -563,7 +563,12 @@ def main():
 
     for _ in range(2):
         e2e_step()
+    clocks_e2e = ClockSampler(local)
+    clocks_e2e.start()
     t_e2e = timed(e2e_step, args.steps)
+    clk_e2e = clocks_e2e.stop()
+    # the host-to-device link on its own (the arena's copies with nothing else running)
+    t_h2d = timed(arena.upload, 3) / 3
 
     # the whole job ends when the slowest rank does
     from gbpowspec.replicas import max_over_ranks
@@ -627,6 +632,7 @@ def main():
         "cpu_baseline": cpu,
         "e2e": {"value": mocks / t_e2e, "unit": "mocks/s", "h2d_bytes_per_step": arena.nbytes,
                 "d2h_bytes_per_step": int(pk_host.numel() * 8),
+                "h2d_alone_gbs": arena.nbytes / t_h2d / 1e9, "clocks": clk_e2e,
                 "path": "BatchRunner.run_from_host (pinned H2D of every mock, chunk by chunk on a copy stream "
                         "overlapping the lanes) + P_l D2H"},
         # per mock: the traced stages (the scan stage is two cub kernels) + lane_begin + lane_end; per batch
