@@ -172,8 +172,10 @@ def kernel_bytes(n: int, N: int, G: int) -> dict:
     M = N ** 3
     Mh = N * N * (N // 2 + 1)
     return {
-        "deposit_count": 12 * n,                  # read x, y, z
-        "deposit_scatter": 12 * n,                # read x, y, z (bucket writes are implementation traffic)
+        # one-pass bucketing: read x, y, z (the bucket writes are implementation traffic); its scan and
+        # scatter return at once unless a bucket overflowed, so they get no byte count
+        "deposit_fill": 12 * n,
+        "deposit_count": 12 * n,                  # count path (small catalogues): read x, y, z
         # deposit fused with the z pass: every particle read once, the z-transformed half spectra written
         # once (the bucket entries it actually reads, 16 B per particle and touched tile, are
         # implementation traffic, as is the spectrum rows' padding)

@@ -92,8 +92,14 @@ typedef struct gbp_deposit_stats {
                            mesh deposit accumulates at 2^s; the fused deposit
                            of gbp_particles_power at 2^(s - t) per tile, t >= 0
                            from the tile's occupancy, its totals shifted to 2^s) */
-  int pad_;
+  int flags;            /* GBP_STATS_* bits below                           */
 } gbp_deposit_stats;
+
+/* flags bit: a tile's bucket outgrew the fixed capacity the one-pass
+ * bucketing gives it (a strongly clustered catalogue), so the buckets were
+ * rebuilt by a scan and a second scatter; the results are the same, the
+ * call took longer. */
+#define GBP_STATS_REFILLED 1
 
 int gbp_deposit_workspace_size(int64_t n_particles, int n_mesh, int mas,
                                int interlace, int compat, size_t* bytes);

@@ -349,8 +349,8 @@ deposit_fftz_kernel(DepGeom g, const float4* __restrict__ entries, const unsigne
   const int t = blockIdx.x;
   const int ty = t % g.nt[1], tx = t / g.nt[1];
   const int x0 = tx * CT::TX, y0 = ty * CT::TY;
-  const unsigned beg = offsets[t];
-  const unsigned end = beg + counts[t * CSTRIDE];
+  unsigned beg, end;
+  tile_range(g, t, counts, offsets, ctr, beg, end);
   const int sg = fixed_scale_exp(ctr->maxw_bits, 0);
   for (int k = tid; k < NSB * N; k += NT) zc[k] = 0;
   __syncthreads();
@@ -407,8 +407,8 @@ deposit_fftz_wide_kernel(DepGeom g, const float4* __restrict__ entries, const un
       for (int k = 0; k < n; ++k) {
         const int tt = s_list[k];
         const int ty = tt % g.nt[1], tx = tt / g.nt[1];
-        const unsigned beg = offsets[tt];
-        const unsigned end = beg + counts[tt * CSTRIDE];
+        unsigned beg, end;
+        tile_range(g, tt, counts, offsets, ctr, beg, end);
         const long long packed = tile_mass[(long long)ntiles + tt];
         int sh[NSB];
 #pragma unroll
@@ -436,7 +436,7 @@ int particles_layout(int64_t n, gbp_fft_plan plan, gbp_bins B, int mas, int ells
   if (!plan || !B || plan->n != B->N) return GBP_ERR_INVALID;
   if (!plan->own || (plan->grids != 1 && plan->grids != 2)) return GBP_ERR_UNSUPPORTED;
   const int tile[3] = {tx, ty, B->N};
-  int st = deposit_layout(n, B->N, mas, plan->grids == 2, GBP_COMPAT_NONE, tile, L.dep);
+  int st = deposit_layout(n, B->N, mas, plan->grids == 2, GBP_COMPAT_NONE, tile, L.dep, true);
   if (st) return st;
   st = xbin_power_workspace(plan, B, ells, &L.xbin);
   if (st) return st;
@@ -503,10 +503,11 @@ int particles_power_n(DepGeom g, int64_t n_launch, gbp_fft_plan plan, gbp_bins B
   int r = particles_layout(n_launch, plan, B, mas, ells, tx, ty, L);
   if (r) return r;
   if (!workspace || ws_bytes < L.total) return GBP_ERR_WORKSPACE;
-  const DepBuffers b = carve_deposit(workspace, L.dep, n_launch);
+  const DepBuffers b = carve_deposit(workspace, L.dep);
   void* xws = static_cast<char*>(workspace) + align256(L.dep.total);
   for (int a = 0; a < 3; ++a) { g.td[a] = L.dep.td[a]; g.ts[a] = L.dep.ts[a]; g.nt[a] = L.dep.nt[a]; }
   g.vec_ok = 0;
+  g.tcap = L.dep.tcap;
   const int G = plan->grids;
   float2* spec = static_cast<float2*>(spectrum);
   GBP_CUDA_TRY(cudaMemsetAsync(b.ctr, 0, zeroed_bytes(L.dep), st));

@@ -18,6 +18,11 @@
 //                      the mesh exactly once.
 //   5. stats_kernel    folds the per-block partial sums in a fixed order.
 //
+// With enough particles per tile, passes 1-3 are one: fill_kernel gives
+// each tile a bucket of fixed capacity and writes every entry at the slot
+// its count atomic returns; scan and scatter (from those counts) run only if
+// a bucket overflowed (deposit_core.cuh, deposit_layout).
+//
 // Integer accumulation makes each cell's sum independent of particle order
 // and scheduling, so the mesh is bitwise reproducible; no float atomics are
 // used.  Every cell is written once (zeros included): no clearing pass.
@@ -51,8 +56,8 @@ deposit_kernel(DepGeom g, const float4* __restrict__ entries, const unsigned* __
   const int x0 = tx * g.td[0], y0 = ty * g.td[1], z0 = tz * g.td[2];
   const int ex = min(g.td[0], g.N - x0), ey = min(g.td[1], g.N - y0), ez = min(g.td[2], g.N - z0);
 
-  const unsigned beg = offsets[t];
-  const unsigned end = beg + counts[t * CSTRIDE];
+  unsigned beg, end;
+  tile_range(g, t, counts, offsets, ctr, beg, end);
   const int s = fixed_scale_exp(ctr->maxw_bits, CM);
   const float sc = ldexpf(1.0f, s);
   const float inv_sc = ldexpf(1.0f, -s);
@@ -156,6 +161,10 @@ deposit_kernel(DepGeom g, const float4* __restrict__ entries, const unsigned* __
   }
 }
 
+// Buckets of a fixed capacity filled in one pass (count, scan and scatter
+// only when one overflows), as on the fused path.
+constexpr bool kMeshFill = true;
+
 template <int MAS, int G, int CM>
 int run_scheme(const DepGeom& g, const DepLayout& L, const DepBuffers& b, const float* mesh_in, float* mesh_out,
                cudaStream_t st) {
@@ -176,8 +185,9 @@ int run_scheme(const DepGeom& g, const DepLayout& L, const DepBuffers& b, const 
 // `n` sizes the launches (the particle count, or a job's capacity).
 int deposit_launch(DepGeom g, const DepLayout& L, int64_t n, int mas, int G, int compat, const float* mesh_in,
                    float* mesh_out, gbp_deposit_stats* stats_out, void* workspace, cudaStream_t stream) {
-  const DepBuffers b = carve_deposit(workspace, L, n);
+  const DepBuffers b = carve_deposit(workspace, L);
   for (int a = 0; a < 3; ++a) { g.td[a] = L.td[a]; g.ts[a] = L.ts[a]; g.nt[a] = L.nt[a]; }
+  g.tcap = L.tcap;
   g.vec_ok = ((reinterpret_cast<uintptr_t>(mesh_out) | reinterpret_cast<uintptr_t>(mesh_in)) & 15u) == 0;
   GBP_CUDA_TRY(cudaMemsetAsync(b.ctr, 0, zeroed_bytes(L), stream));
   int st;
@@ -212,7 +222,7 @@ extern "C" int gbp_deposit_workspace_size(int64_t n, int N, int mas, int interla
                                           size_t* bytes) {
   if (!bytes) return GBP_ERR_INVALID;
   DepLayout L;
-  const int st = deposit_layout(n, N, mas, interlace, compat, kCubeTiles, L);
+  const int st = deposit_layout(n, N, mas, interlace, compat, kCubeTiles, L, kMeshFill);
   if (st) return st;
   *bytes = L.total;
   return GBP_OK;
@@ -224,7 +234,7 @@ extern "C" int gbp_deposit(const float* x, const float* y, const float* z, const
                            gbp_deposit_stats* stats_out, void* workspace, size_t ws_bytes,
                            gbp_stream_t stream_) {
   DepLayout L;
-  const int st = deposit_layout(n, N, mas, interlace, compat, kCubeTiles, L);
+  const int st = deposit_layout(n, N, mas, interlace, compat, kCubeTiles, L, kMeshFill);
   if (st) return st;
   if (!mesh_out) return GBP_ERR_INVALID;
   if (n > 0 && (!x || !y || !z)) return GBP_ERR_INVALID;
@@ -242,7 +252,7 @@ extern "C" int gbp_deposit_job(const gbp_job* job, int64_t capacity, int N, int 
                                float* mesh_out, gbp_deposit_stats* stats_out, void* workspace, size_t ws_bytes,
                                gbp_stream_t stream_) {
   DepLayout L;
-  const int st = deposit_layout(capacity, N, mas, interlace, GBP_COMPAT_NONE, kCubeTiles, L);
+  const int st = deposit_layout(capacity, N, mas, interlace, GBP_COMPAT_NONE, kCubeTiles, L, kMeshFill);
   if (st) return st;
   if (!job || !mesh_out) return GBP_ERR_INVALID;
   if (!workspace || ws_bytes < L.total) return GBP_ERR_WORKSPACE;

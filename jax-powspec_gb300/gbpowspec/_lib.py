@@ -41,11 +41,13 @@ class DepositStats(C.Structure):
         ("n_kept", C.c_longlong),
         ("n_nonfinite", C.c_longlong),
         ("scale_exp", C.c_int),
-        ("pad_", C.c_int),
+        ("flags", C.c_int),
     ]
 
 
 STATS_BYTES = C.sizeof(DepositStats)
+STATS_REFILLED = 1          # gbp_deposit_stats.flags: the buckets outgrew their one-pass capacity
+STATS_RESULT_BYTES = DepositStats.flags.offset   # the statistics proper (flags say how they were computed)
 
 
 class Job(C.Structure):

@@ -61,6 +61,7 @@ def test_batch_equals_single_mock_pipeline(graphs):
 def test_alone_and_in_the_mix_are_identical():
     """One mock alone on one lane vs the same mock inside a mixed batch on 4 lanes, twice."""
     from gbpowspec.batch import BatchRunner, ParticleArena
+    from gbpowspec import _lib
     N = 64
     boxes = np.array([500.0, 900.0, 700.0, 1200.0, 650.0, 800.0, 1000.0])
     sizes = [20_000, 70_000, 35_000, 9_000, 64_000, 50_000, 27_000]
@@ -80,7 +81,8 @@ def test_alone_and_in_the_mix_are_identical():
     torch.cuda.synchronize()
     assert _same(a.pk, b.pk) and _same(a.pk, one.pk)
     assert _same(a.kmean, one.kmean)
-    assert torch.equal(a.stats, one.stats)
+    R = _lib.STATS_RESULT_BYTES
+    assert torch.equal(a.stats[:, :R], one.stats[:, :R])
     assert torch.equal(a.nmodes, one.nmodes)
 
 
@@ -150,6 +152,7 @@ def test_tune_lanes_returns_a_candidate():
 def test_run_from_host_matches_upload_then_run():
     """Chunked uploads overlapping the lanes give the same bits as one upload before the batch."""
     from gbpowspec.batch import BatchRunner, ParticleArena
+    from gbpowspec import _lib
     N, box = 64, 600.0
     sizes = [30_000, 12_000, 45_000, 8_000, 27_000, 39_000, 16_000]
     cats = _cats(sizes, box, seed0=700)
@@ -163,5 +166,7 @@ def test_run_from_host_matches_upload_then_run():
     for chunk in (None, 1, 2, 5):
         got = runner.run_from_host(arena, jobs, chunk=chunk)
         torch.cuda.synchronize()
-        assert _same(got.pk, want.pk) and torch.equal(got.nmodes, want.nmodes) and torch.equal(got.stats, want.stats)
+        R = _lib.STATS_RESULT_BYTES
+        assert _same(got.pk, want.pk) and torch.equal(got.nmodes, want.nmodes)
+        assert torch.equal(got.stats[:, :R], want.stats[:, :R])
     runner.close()

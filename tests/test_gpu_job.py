@@ -52,7 +52,8 @@ def test_deposit_job_matches_deposit(mas, interlace):
         assert st == 0, _lib.strerror(st)
         torch.cuda.synchronize()
         assert torch.equal(mesh, want)
-        assert bytes(_native.read_stats(stats)) == bytes(_native.read_stats(want_stats))
+        R = _lib.STATS_RESULT_BYTES
+        assert bytes(_native.read_stats(stats))[:R] == bytes(_native.read_stats(want_stats))[:R]
 
 
 def test_deposit_job_clamps_to_capacity():
