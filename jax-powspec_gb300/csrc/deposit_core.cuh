@@ -526,17 +526,37 @@ stats_kernel(const DepCounters* ctr, const float4* block_stats, const uint2* blo
   __shared__ long long s_m[2][32], s_c[2][32];
   ff a{0.f, 0.f}, b{0.f, 0.f};
   long long kept = 0, bad = 0, m0 = 0, m1 = 0;
-  for (int k = threadIdx.x; k < nblocks; k += blockDim.x) {
-    const float4 v = block_stats[k];
-    a = ff_add(a, ff{v.x, v.y});
-    b = ff_add(b, ff{v.z, v.w});
-    const uint2 c = block_counts[k];
-    kept += c.x;
-    bad += c.y;
+  // a thread adds blocks k = tid, tid + blockDim, ... in that order; the loads of SU of them are issued
+  // before the adds
+  constexpr int SU = 4;
+  const int nt = blockDim.x;
+  for (int k0 = threadIdx.x; k0 < nblocks; k0 += SU * nt) {
+    float4 v[SU];
+    uint2 c[SU];
+#pragma unroll
+    for (int u = 0; u < SU; ++u) {
+      const int k = k0 + u * nt;
+      v[u] = k < nblocks ? block_stats[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+      c[u] = k < nblocks ? block_counts[k] : make_uint2(0u, 0u);
+    }
+#pragma unroll
+    for (int u = 0; u < SU; ++u) {
+      if (k0 + u * nt >= nblocks) break;
+      a = ff_add(a, ff{v[u].x, v[u].y});
+      b = ff_add(b, ff{v[u].z, v[u].w});
+      kept += c[u].x;
+      bad += c[u].y;
+    }
   }
-  for (int k = threadIdx.x; k < ntiles; k += blockDim.x) {
-    m0 += tile_mass[k];
-    if (G == 2) m1 += tile_mass[ntiles + k];
+  for (int k0 = threadIdx.x; k0 < ntiles; k0 += SU * nt) {       // integers: any order
+#pragma unroll
+    for (int u = 0; u < SU; ++u) {
+      const int k = k0 + u * nt;
+      if (k < ntiles) {
+        m0 += tile_mass[k];
+        if (G == 2) m1 += tile_mass[ntiles + k];
+      }
+    }
   }
   a = warp_ff_sum(a);
   b = warp_ff_sum(b);

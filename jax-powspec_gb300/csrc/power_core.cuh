@@ -201,17 +201,35 @@ __device__ __forceinline__ void fold_bin(const float2* __restrict__ part_ff, int
                                          double (&m)[MAXV]) {
   __shared__ ff s_w[MAXV][FOLD_THREADS / 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int q = 0; q < NV; ++q) {
-    ff acc{0.f, 0.f};
-    for (int c = threadIdx.x; c < C; c += FOLD_THREADS) {
-      const float2 v = part_ff[((long long)c * NV + q) * nbe + b];
-      acc = ff_add(acc, ff{v.x, v.y});
-    }
+  // a thread adds partials c = tid, tid + FOLD_THREADS, ... in that order; the loads of FU of them
+  // (every moment) are issued before the adds
+  constexpr int FU = 4;
+  ff acc[MAXV];
+#pragma unroll
+  for (int q = 0; q < MAXV; ++q) acc[q] = ff{0.f, 0.f};
+  for (int c0 = threadIdx.x; c0 < C; c0 += FU * FOLD_THREADS) {
+    float2 v[MAXV][FU];
+#pragma unroll
+    for (int q = 0; q < MAXV; ++q)
+#pragma unroll
+      for (int u = 0; u < FU; ++u) {
+        const int c = c0 + u * FOLD_THREADS;
+        v[q][u] = (q < NV && c < C) ? part_ff[((long long)c * NV + q) * nbe + b] : make_float2(0.f, 0.f);
+      }
+#pragma unroll
+    for (int q = 0; q < MAXV; ++q)
+#pragma unroll
+      for (int u = 0; u < FU; ++u)
+        if (q < NV && c0 + u * FOLD_THREADS < C) acc[q] = ff_add(acc[q], ff{v[q][u].x, v[q][u].y});
+  }
+#pragma unroll
+  for (int q = 0; q < MAXV; ++q) {
+    if (q >= NV) break;
     for (int o = 16; o > 0; o >>= 1) {
-      ff t{__shfl_xor_sync(0xffffffffu, acc.hi, o), __shfl_xor_sync(0xffffffffu, acc.lo, o)};
-      acc = ff_add(acc, t);
+      ff t{__shfl_xor_sync(0xffffffffu, acc[q].hi, o), __shfl_xor_sync(0xffffffffu, acc[q].lo, o)};
+      acc[q] = ff_add(acc[q], t);
     }
-    if (lane == 0) s_w[q][warp] = acc;
+    if (lane == 0) s_w[q][warp] = acc[q];
   }
   __syncthreads();
   if (threadIdx.x == 0) {
