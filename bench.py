@@ -148,6 +148,8 @@ def run_reference_arm(args):
         "steps": steps, "warmup": warm, "ms_per_step": t / steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded lognormal mock)",
         "config": {**_cfg_json(), "mas": "cic", "interlace": False, "grids": 1, "ells": [0, 2, 4],
+                   "workload": CONFIG["workload"].replace("TSC+interlaced", "CIC one grid (the reference's "
+                                                          "scheme) on the same catalogue"),
                    "implementation": "numpy stand-in (oracle/reference_fast) for the reference's own path: "
                    "src/mas.py cic_mas_vec (CIC with its corner-weight bug, one grid) -> delta/mean - 1 -> "
                    "src/correlations.py powspec_vec (float32 histograms); JAX is not installed on this host",

@@ -118,9 +118,9 @@ __device__ __forceinline__ long long tile_grid(const DepGeom& g, const float4* _
   for (unsigned i = beg + tid; i < end; i += NT) {
     const float4 e = entries[i];
     Axis<R> ax, ay, az;
-    make_axis<MAS, 0>(g, e.x, grid, ax);
-    make_axis<MAS, 0>(g, e.y, grid, ay);
-    make_axis<MAS, 0>(g, e.z, grid, az);
+    make_axis<MAS, 0, N>(g, e.x, grid, ax);
+    make_axis<MAS, 0, N>(g, e.y, grid, ay);
+    make_axis<MAS, 0, N>(g, e.z, grid, az);
     int lx[R], ly[R], zz[R];
     local_nodes<R>(ax, N, x0, TX, lx);
     local_nodes<R>(ay, N, y0, TY, ly);
@@ -283,12 +283,12 @@ __device__ __forceinline__ bool block_scales(const DepGeom& g, const float4* __r
           continue;
         }
         Axis<R> a0;
-        make_axis<MAS, 0>(g, a == 0 ? e.x : (a == 1 ? e.y : e.z), 0, a0);
+        make_axis<MAS, 0, N>(g, a == 0 ? e.x : (a == 1 ? e.y : e.z), 0, a0);
         first[a] = a0.first;
         last[a] = a0.first + R - 1;
         if constexpr (G == 2) {
           Axis<R> a1;
-          make_axis<MAS, 0>(g, a == 0 ? e.x : (a == 1 ? e.y : e.z), 1, a1);
+          make_axis<MAS, 0, N>(g, a == 0 ? e.x : (a == 1 ? e.y : e.z), 1, a1);
           last[a] = a1.first + R - 1;
         }
       }

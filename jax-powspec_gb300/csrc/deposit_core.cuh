@@ -84,12 +84,16 @@ struct Axis {
 
 // B-spline of order MAS with nodes at integer grid coordinates (the
 // reference's node convention: node i sits at xmin + i*H).  `half` shifts
-// the particle by +half a cell (the second, interlaced grid).
-template <int MAS>
+// the particle by +half a cell (the second, interlaced grid).  NC > 0: the
+// mesh side as a power-of-two constant (the cell index wraps with a mask,
+// the same value as pmod for every int).
+template <int MAS, int NC = 0>
 __device__ __forceinline__ void axis_bspline(float u, int N, int half, Axis<MAS>& a) {
+  static_assert(NC == 0 || (NC & (NC - 1)) == 0, "NC is a power of two");
   const float fu = floorf(u);
   float d = __fsub_rn(u, fu);                 // exact, in [0, 1)
-  int i = pmod(__float2int_rz(fu), N);
+  const int i0 = __float2int_rz(fu);
+  int i = NC ? (i0 & (NC - 1)) : wrap_index(i0, N);
   if (half) {
     d = __fadd_rn(d, 0.5f);
     if (d >= 1.0f) { d = __fsub_rn(d, 1.0f); i += 1; }
@@ -139,7 +143,7 @@ __device__ __forceinline__ void axis_compat(float u, int N, int wrap, Axis<2>& a
   int ixp = ix + 1;
   float dh = d;
   if (CM == GBP_COMPAT_VEC) {
-    if (wrap) ixp = pmod(ixp + N, N);
+    if (wrap) ixp = wrap_index(ixp, N);         // = pmod(ixp + N, N): |ixp| < 2^30 + 1
     else if (ixp >= N) ixp = 0;
   } else {
     if (wrap) { if (ixp >= N) ixp -= N; }
@@ -156,10 +160,10 @@ __device__ __forceinline__ void axis_compat(float u, int N, int wrap, Axis<2>& a
   a.w[1] = dh;
 }
 
-template <int MAS, int CM>
+template <int MAS, int CM, int NC = 0>
 __device__ __forceinline__ void make_axis(const DepGeom& g, float u, int grid, Axis<Scheme<MAS, CM>::R>& a) {
   if constexpr (CM != 0) axis_compat<CM>(u, g.N, g.wrap, a);
-  else axis_bspline<MAS>(u, g.N, grid, a);
+  else axis_bspline<MAS, NC>(u, g.N, grid, a);
 }
 
 // The particles of one thread in count/scatter: loads issued together.

@@ -67,6 +67,10 @@ __host__ __device__ inline int pmod(int a, int n) {
   return r < 0 ? r + n : r;
 }
 
+// pmod for an index that is usually in [0, n) already: one compare on that
+// path instead of an integer division.
+__host__ __device__ inline int wrap_index(int a, int n) { return (unsigned)a < (unsigned)n ? a : pmod(a, n); }
+
 // Signed wavenumber of FFT index i on an n-point axis, as the reference
 // builds it: ki = i if i <= n/2 else i - n (src/correlations.py:25).
 __host__ __device__ inline int signed_k(int i, int n) { return i > n / 2 ? i - n : i; }
