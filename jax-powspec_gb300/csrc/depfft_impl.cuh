@@ -340,6 +340,7 @@ __global__ void __launch_bounds__(CT::NT, CT::MINB)
 deposit_fftz_kernel(DepGeom g, const float4* __restrict__ entries, const unsigned* __restrict__ counts,
                     const unsigned* __restrict__ offsets, const DepCounters* ctr, const float2* __restrict__ tw,
                     float2* __restrict__ spec, long long* __restrict__ tile_mass) {
+  pdl_wait();
   constexpr int NPEN = CT::NPEN, NT = CT::NT, NSB = CT::NSB;
   extern __shared__ __align__(16) int acc_smem[];
   int* zc = acc_smem + NPEN * N;                       // [NSB][N] entries covering each block's planes
@@ -384,6 +385,7 @@ __global__ void __launch_bounds__(CT::NT, CT::MINB)
 deposit_fftz_wide_kernel(DepGeom g, const float4* __restrict__ entries, const unsigned* __restrict__ counts,
                          const unsigned* __restrict__ offsets, const DepCounters* ctr, const float2* __restrict__ tw,
                          float2* __restrict__ spec, long long* __restrict__ tile_mass, int ntiles) {
+  pdl_wait();
   constexpr int NT = CT::NT, NSB = CT::NSB;
   extern __shared__ __align__(16) unsigned long long wide_smem[];
   __shared__ long long s_part[NT / 32];
@@ -453,8 +455,8 @@ int run_fused(const DepGeom& g, const DepLayout& L, const DepBuffers& b, const f
   GBP_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CT::SMEM));
   {
     GBP_TRACE("deposit_fft_z", st);
-    k<<<L.ntiles, CT::NT, CT::SMEM, st>>>(g, b.entries, b.counts, b.offsets, b.ctr, tw, spec, b.tile_mass);
-    GBP_LAUNCH_CHECK();
+    GBP_CUDA_TRY(launch_pdl(k, dim3(L.ntiles), dim3(CT::NT), CT::SMEM, st, g, b.entries, b.counts, b.offsets, b.ctr,
+                            tw, spec, b.tile_mass));
   }
   // tiles of dense clumps, if any, with 64-bit cells (as many CTAs as fit at once scan the marks: a
   // dense small mesh can send most of its tiles here)
@@ -465,9 +467,9 @@ int run_fused(const DepGeom& g, const DepLayout& L, const DepBuffers& b, const f
   GBP_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   GBP_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kw, CT::NT, CT::SMEM_WIDE));
   GBP_TRACE("deposit_fft_z_wide", st);
-  kw<<<std::max(1, std::min(sms * std::max(per_sm, 1), L.ntiles)), CT::NT, CT::SMEM_WIDE, st>>>(
-      g, b.entries, b.counts, b.offsets, b.ctr, tw, spec, b.tile_mass, L.ntiles);
-  GBP_LAUNCH_CHECK();
+  GBP_CUDA_TRY(launch_pdl(kw, dim3(std::max(1, std::min(sms * std::max(per_sm, 1), L.ntiles))), dim3(CT::NT),
+                          CT::SMEM_WIDE, st, g, b.entries, b.counts, b.offsets, b.ctr, tw, spec, b.tile_mass,
+                          L.ntiles));
   return GBP_OK;
 }
 

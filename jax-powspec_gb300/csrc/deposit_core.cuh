@@ -285,6 +285,7 @@ template <int MAS, int G, int CM>
 __global__ void __launch_bounds__(CNT_THREADS)
 count_kernel(DepGeom gp, unsigned* __restrict__ counts, DepCounters* ctr, float4* block_stats,
              uint2* block_counts) {
+  pdl_wait();
   DepGeom g = gp;
   resolve_job(g);
   float maxw = 0.0f;
@@ -327,6 +328,7 @@ template <int MAS, int G, int CM>
 __global__ void __launch_bounds__(CNT_THREADS, 4)
 fill_kernel(DepGeom gp, unsigned* __restrict__ counts, float4* __restrict__ entries, DepCounters* ctr,
             float4* block_stats, uint2* block_counts) {
+  pdl_wait();
   DepGeom g = gp;
   resolve_job(g);
   const unsigned tcap = g.tcap;
@@ -392,6 +394,7 @@ constexpr int FSCAN_THREADS = 1024;
 __global__ void __launch_bounds__(FSCAN_THREADS)
 gated_scan_kernel(const unsigned* __restrict__ counts, unsigned* __restrict__ offsets, int ntiles,
                   const DepCounters* ctr) {
+  pdl_wait();
   if (ctr->overflow == 0u) return;
   __shared__ unsigned s_warp[FSCAN_THREADS / 32];
   const int per = (ntiles + FSCAN_THREADS - 1) / FSCAN_THREADS;
@@ -437,6 +440,7 @@ template <int MAS, int G, int CM>
 __global__ void __launch_bounds__(CNT_THREADS, 4)
 scatter_kernel(DepGeom gp, const unsigned* __restrict__ offsets, unsigned* __restrict__ fills,
                float4* __restrict__ entries, const DepCounters* gate) {
+  pdl_wait();
   if (gate && gate->overflow == 0u) return;            // fill path: the buckets are complete
   DepGeom g = gp;
   resolve_job(g);
@@ -526,6 +530,7 @@ constexpr int STATS_THREADS = 1024;
 __global__ void __launch_bounds__(STATS_THREADS)
 stats_kernel(const DepCounters* ctr, const float4* block_stats, const uint2* block_counts, int nblocks,
              const long long* tile_mass, int ntiles, int compat, int G, gbp_deposit_stats* out) {
+  pdl_wait();
   __shared__ ff s_a[32], s_b[32];
   __shared__ long long s_m[2][32], s_c[2][32];
   ff a{0.f, 0.f}, b{0.f, 0.f};
@@ -733,27 +738,26 @@ int bucket_particles(const DepGeom& g, const DepLayout& L, const DepBuffers& b, 
     // fill path: one pass; the scan and the scatter return at once unless a bucket overflowed
     if (L.nblocks > 0) {
       GBP_TRACE("deposit_fill", st);
-      fill_kernel<MAS, G, CM><<<L.nblocks, CNT_THREADS, 0, st>>>(g, b.counts, b.entries, b.ctr, b.block_stats,
-                                                                  b.block_counts);
-      GBP_LAUNCH_CHECK();
+      GBP_CUDA_TRY(launch_pdl(fill_kernel<MAS, G, CM>, dim3(L.nblocks), dim3(CNT_THREADS), 0, st, g, b.counts,
+                              b.entries, b.ctr, b.block_stats, b.block_counts));
     }
     {
       GBP_TRACE("deposit_scan", st);
-      gated_scan_kernel<<<1, FSCAN_THREADS, 0, st>>>(b.counts, b.offsets, L.ntiles, b.ctr);
-      GBP_LAUNCH_CHECK();
+      GBP_CUDA_TRY(launch_pdl(gated_scan_kernel, dim3(1), dim3(FSCAN_THREADS), 0, st, b.counts, b.offsets,
+                              L.ntiles, b.ctr));
     }
     if (L.nblocks > 0) {
       GBP_TRACE("deposit_scatter", st);
-      scatter_kernel<MAS, G, CM><<<std::min(L.nblocks, FILL_SCATTER_BLOCKS), CNT_THREADS, 0, st>>>(
-          g, b.offsets, b.fills, b.entries, b.ctr);
-      GBP_LAUNCH_CHECK();
+      GBP_CUDA_TRY(launch_pdl(scatter_kernel<MAS, G, CM>, dim3(std::min(L.nblocks, FILL_SCATTER_BLOCKS)),
+                              dim3(CNT_THREADS), 0, st, g, b.offsets, b.fills, b.entries,
+                              static_cast<const DepCounters*>(b.ctr)));
     }
     return GBP_OK;
   }
   if (L.nblocks > 0) {
     GBP_TRACE("deposit_count", st);
-    count_kernel<MAS, G, CM><<<L.nblocks, CNT_THREADS, 0, st>>>(g, b.counts, b.ctr, b.block_stats, b.block_counts);
-    GBP_LAUNCH_CHECK();
+    GBP_CUDA_TRY(launch_pdl(count_kernel<MAS, G, CM>, dim3(L.nblocks), dim3(CNT_THREADS), 0, st, g, b.counts, b.ctr,
+                            b.block_stats, b.block_counts));
   }
   {
     GBP_TRACE("deposit_scan", st);
@@ -763,8 +767,8 @@ int bucket_particles(const DepGeom& g, const DepLayout& L, const DepBuffers& b, 
   }
   if (L.nblocks > 0) {
     GBP_TRACE("deposit_scatter", st);
-    scatter_kernel<MAS, G, CM><<<L.nblocks, CNT_THREADS, 0, st>>>(g, b.offsets, b.fills, b.entries, nullptr);
-    GBP_LAUNCH_CHECK();
+    GBP_CUDA_TRY(launch_pdl(scatter_kernel<MAS, G, CM>, dim3(L.nblocks), dim3(CNT_THREADS), 0, st, g, b.offsets,
+                            b.fills, b.entries, static_cast<const DepCounters*>(nullptr)));
   }
   return GBP_OK;
 }
@@ -772,9 +776,9 @@ int bucket_particles(const DepGeom& g, const DepLayout& L, const DepBuffers& b, 
 inline int deposit_stats(const DepBuffers& b, const DepLayout& L, int compat, int G, gbp_deposit_stats* out,
                          cudaStream_t st) {
   GBP_TRACE("deposit_stats", st);
-  stats_kernel<<<1, STATS_THREADS, 0, st>>>(b.ctr, b.block_stats, b.block_counts, L.nblocks, b.tile_mass, L.ntiles,
-                                            compat, G, out);
-  GBP_LAUNCH_CHECK();
+  GBP_CUDA_TRY(launch_pdl(stats_kernel, dim3(1), dim3(STATS_THREADS), 0, st, static_cast<const DepCounters*>(b.ctr),
+                          static_cast<const float4*>(b.block_stats), static_cast<const uint2*>(b.block_counts),
+                          L.nblocks, static_cast<const long long*>(b.tile_mass), L.ntiles, compat, G, out));
   return GBP_OK;
 }
 

@@ -106,6 +106,7 @@ template <int N>
 __global__ void __launch_bounds__(N / 2, N <= 512 ? 4 : 2)
 fft_cols_kernel(float2* __restrict__ data, long long plane_stride, long long row_stride, int nplanes, int nkb,
                 const float2* __restrict__ tw) {
+  pdl_wait();
   extern __shared__ __align__(16) float2 s[];
   const int plane = blockIdx.x / nkb, kb = blockIdx.x % nkb;
   if (plane >= nplanes) return;
@@ -143,8 +144,8 @@ int run_fft(const float* mesh, float2* spec, int G, const float2* tw, cudaStream
   GBP_CUDA_TRY(cudaFuncSetAttribute(kc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   {  // y pass: a plane is one x slab of one grid; rows (y) are P apart
     GBP_TRACE("fft_y", st);
-    kc<<<(unsigned)(G * N * nkb), N / 2, smem, st>>>(spec, (long long)N * P, P, G * N, nkb, tw);
-    GBP_LAUNCH_CHECK();
+    GBP_CUDA_TRY(launch_pdl(kc, dim3((unsigned)(G * N * nkb)), dim3(N / 2), smem, st, spec, (long long)N * P,
+                            (long long)P, G * N, nkb, tw));
   }
   // x pass: a plane is one y row of one grid; rows (x) are N*P apart
   for (int g = 0; x_pass && g < G; ++g) {

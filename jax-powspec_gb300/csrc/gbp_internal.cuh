@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <stdlib.h>
 
 #include "gbpowspec.h"
 
@@ -45,6 +46,42 @@ class TraceScope {
   int slot_;
   cudaStream_t s_;
 };
+
+// Programmatic dependent launch.  A kernel launched with launch_pdl is
+// set up while the kernel before it in the stream finishes (its launch
+// latency hides behind that kernel's last blocks); it must call pdl_wait()
+// before it touches global memory, which returns once the previous kernel
+// has completed and its writes are visible.  Launched the ordinary way,
+// pdl_wait() is a no-op.  No kernel triggers its dependents early
+// (griddepcontrol.launch_dependents): blocks waiting from the start hold SM
+// slots, which cost 3 % on 128^3 batch lanes where the implicit trigger at
+// completion gains 3 % (one mock at a time: 2 % at 128^3, 1 % at 512^3).
+// GBP_PDL=0 in the environment turns the attribute off.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+inline bool pdl_enabled() {
+  static const bool on = [] {
+    const char* e = getenv("GBP_PDL");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                       Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl_enabled() ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
 
 // Bytes rounded up to a multiple of 256 (keeps every workspace slice aligned).
 inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }

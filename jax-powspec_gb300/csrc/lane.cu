@@ -70,6 +70,7 @@ namespace {
 __global__ void lane_set_desc(LaneDesc* d, LaneDesc v) { *d = v; }
 
 __global__ void lane_begin(LaneDesc* d, gbp_job* slot) {
+  pdl_wait();
   const int idx = d->next;
   const bool active = idx >= 0 && idx < d->n_jobs;
   static_assert(sizeof(gbp_job) % 4 == 0, "job copied as 32-bit words");
@@ -86,6 +87,7 @@ __global__ void lane_begin(LaneDesc* d, gbp_job* slot) {
 
 __global__ void lane_end(LaneDesc* d, int nb, const double* pk, const double* kmean, const long long* nmodes,
                          const gbp_deposit_stats* stats) {
+  pdl_wait();
   const int idx = d->next;
   if (d->active) {
     const gbp_lane_out o = d->out;
@@ -160,9 +162,8 @@ int lane_sequence(gbp_lane L, cudaStream_t st) {
                               (L->ells & GBP_KSUM) ? L->kmean : nullptr, s);
   if (r) return r;
   GBP_TRACE("lane_end", st);
-  lane_end<<<1, 256, 0, st>>>(L->desc, L->nb, L->pk, (L->ells & GBP_KSUM) ? L->kmean : nullptr, L->nmodes,
-                              L->stats);
-  GBP_LAUNCH_CHECK();
+  GBP_CUDA_TRY(launch_pdl(lane_end, dim3(1), dim3(256), 0, st, L->desc, L->nb, L->pk,
+                          (L->ells & GBP_KSUM) ? L->kmean : nullptr, L->nmodes, L->stats));
   return GBP_OK;
 }
 

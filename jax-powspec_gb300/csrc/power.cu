@@ -236,6 +236,7 @@ __global__ void power_normalize_kernel(const double* sums, const long long* nmod
                                        double norm_delta, double box3, double kf, const double* mass,
                                        const gbp_deposit_stats* stats, int subtract_shot, double* pk_out,
                                        double* kmean_out, const gbp_job* job, int N) {
+  pdl_wait();
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= nb) return;
   if (job) {                      // box size from the device job descriptor
@@ -400,9 +401,9 @@ extern "C" int gbp_power_normalize(const double* sums, const long long* nmodes, 
   const double box3 = box * box * box;
   const double kf = 2.0 * M_PI / box;
   GBP_TRACE("power_normalize", stream);
-  power_normalize_kernel<<<(nb + 127) / 128, 128, 0, stream>>>(sums, nmodes, ksum, nb, norm_delta, box3, kf, mass,
-                                                               stats, subtract_shot, pk_out, kmean_out, nullptr, N);
-  GBP_LAUNCH_CHECK();
+  GBP_CUDA_TRY(launch_pdl(power_normalize_kernel, dim3((nb + 127) / 128), dim3(128), 0, stream, sums, nmodes, ksum,
+                          nb, norm_delta, box3, kf, mass, stats, subtract_shot, pk_out, kmean_out,
+                          static_cast<const gbp_job*>(nullptr), N));
   return GBP_OK;
 }
 
@@ -413,9 +414,8 @@ extern "C" int gbp_power_normalize_job(const double* sums, const long long* nmod
   cudaStream_t stream = reinterpret_cast<cudaStream_t>(stream_);
   if (!sums || !nmodes || !pk_out || !job || nb < 1 || N < 1) return GBP_ERR_INVALID;
   GBP_TRACE("power_normalize", stream);
-  power_normalize_kernel<<<(nb + 127) / 128, 128, 0, stream>>>(sums, nmodes, ksum, nb, 0.0, 0.0, 0.0, mass, stats,
-                                                               subtract_shot, pk_out, kmean_out, job, N);
-  GBP_LAUNCH_CHECK();
+  GBP_CUDA_TRY(launch_pdl(power_normalize_kernel, dim3((nb + 127) / 128), dim3(128), 0, stream, sums, nmodes, ksum,
+                          nb, 0.0, 0.0, 0.0, mass, stats, subtract_shot, pk_out, kmean_out, job, N));
   return GBP_OK;
 }
 

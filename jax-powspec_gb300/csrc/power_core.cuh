@@ -247,6 +247,7 @@ __global__ void __launch_bounds__(FOLD_THREADS)
 power_reduce_kernel(const float2* __restrict__ part_ff, int C, int NV, int nb, int nbe,
                     const long long* __restrict__ plan_nmodes, const double* __restrict__ plan_ksum,
                     double* sums_out, long long* nmodes_out, double* ksum_out) {
+  pdl_wait();
   const int b = blockIdx.x;
   if (b >= nb) return;                         // uniform over the block
   double m[3] = {0.0, 0.0, 0.0};

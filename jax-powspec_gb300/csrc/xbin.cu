@@ -284,6 +284,7 @@ __device__ __forceinline__ void xbin_item(const PowGeom& g, const Smem& t, const
 template <int N, int NV, bool INTER>
 __global__ void __launch_bounds__(XB_THREADS, N >= 1024 ? 1 : 2)
 xbin_kernel(PowGeom g) {
+  pdl_wait();
   constexpr int G = INTER ? 2 : 1;
   constexpr int P = N / 2 + 8;                              // z row pitch of the own transform
   constexpr int TST = XLayout<N>::TST;
@@ -363,8 +364,7 @@ int launch_xbin(const PowGeom& g, size_t smem, cudaStream_t st) {
   // as fast as the persistent grid at 512^3 (0.775 against 0.781 ms)
   const int grid = std::max(1, g.groups);
   GBP_TRACE("fft_x_bins", st);
-  k<<<grid, XB_THREADS, smem, st>>>(g);
-  GBP_LAUNCH_CHECK();
+  GBP_CUDA_TRY(launch_pdl(k, dim3(grid), dim3(XB_THREADS), smem, st, g));
   return GBP_OK;
 }
 
@@ -443,10 +443,10 @@ int xbin_power(gbp_fft_plan plan, float2* spec, gbp_bins B, int mas_order, int e
   }
   if (r) return r;
   GBP_TRACE("power_reduce", st);
-  power_reduce_kernel<<<B->nb, FOLD_THREADS, 0, st>>>(
-      g.part_ff, L.groups, L.NV, B->nb, B->nbe, B->d_nmodes, B->d_ksum, sums_out, nmodes_out,
-      (ells & GBP_KSUM) ? ksum_out : nullptr);
-  GBP_LAUNCH_CHECK();
+  GBP_CUDA_TRY(launch_pdl(power_reduce_kernel, dim3(B->nb), dim3(FOLD_THREADS), 0, st,
+                          static_cast<const float2*>(g.part_ff), L.groups, L.NV, B->nb, B->nbe,
+                          static_cast<const long long*>(B->d_nmodes), static_cast<const double*>(B->d_ksum), sums_out,
+                          nmodes_out, (ells & GBP_KSUM) ? ksum_out : nullptr));
   return GBP_OK;
 }
 
