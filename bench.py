@@ -659,10 +659,12 @@ def main():
 # independent) and reads its bucket entries (0.037 GB at 1,048,576
 # particles, in proportion to the particles): 1.047 + 4 x 0.037 GB for the
 # 4,194,304-particle workload.
+# The one-pass bucketing's entries are still in L2 when it ends (their DRAM
+# writes fall in the deposit/z kernel's window), so it gets no figure.
 PROFILED_TRAFFIC = {
-    ("deposit_fft_z", 512, 4_194_304): 1_046_606_000 + 4 * 37_221_000,
-    ("fft_y", 512, 4_194_304): 1_107_357_000 + 1_053_285_000,
-    ("fft_x_bins", 512, 4_194_304): 1_107_393_000 + 6_821_000,
+    ("deposit_fft_z", 512, 4_194_304): 1_046_520_000 + 4 * 37_453_000,
+    ("fft_y", 512, 4_194_304): 1_107_458_000 + 1_053_273_000,
+    ("fft_x_bins", 512, 4_194_304): 1_107_381_000 + 5_776_000,
 }
 
 
