@@ -46,6 +46,7 @@ __global__ void __launch_bounds__(DEP_THREADS)
 deposit_kernel(DepGeom g, const float4* __restrict__ entries, const unsigned* __restrict__ counts,
                const unsigned* __restrict__ offsets, const DepCounters* ctr, const float* __restrict__ mesh_in,
                float* __restrict__ mesh_out, long long* __restrict__ tile_mass) {
+  pdl_wait();
   constexpr int R = Scheme<MAS, CM>::R;
   extern __shared__ __align__(16) unsigned acc32[];
   __shared__ long long s_part[DEP_THREADS / 32];
@@ -175,9 +176,8 @@ int run_scheme(const DepGeom& g, const DepLayout& L, const DepBuffers& b, const 
   GBP_CUDA_TRY(cudaFuncSetAttribute(deposit_kernel<MAS, G, CM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)smem));
   GBP_TRACE("deposit_tiles", st);
-  deposit_kernel<MAS, G, CM><<<L.ntiles, DEP_THREADS, smem, st>>>(g, b.entries, b.counts, b.offsets, b.ctr, mesh_in,
-                                                                 mesh_out, b.tile_mass);
-  GBP_LAUNCH_CHECK();
+  GBP_CUDA_TRY(launch_pdl(deposit_kernel<MAS, G, CM>, dim3(L.ntiles), dim3(DEP_THREADS), smem, st, g, b.entries,
+                          b.counts, b.offsets, b.ctr, mesh_in, mesh_out, b.tile_mass));
   return GBP_OK;
 }
 

@@ -47,6 +47,7 @@ template <int N, int PAIRS>
 __global__ void __launch_bounds__(PAIRS * N / 16)
 fftz_kernel(const float* __restrict__ mesh, float2* __restrict__ out, long long npencils,
             const float2* __restrict__ tw) {
+  pdl_wait();
   constexpr int NT = PAIRS * N / 16;
   constexpr int CP = PAIRS / 2;
   constexpr int P = zpitch(N);
@@ -135,8 +136,7 @@ int run_fft(const float* mesh, float2* spec, int G, const float2* tw, cudaStream
     GBP_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const long long blocks = (npen + 2 * PAIRS - 1) / (2 * PAIRS);
     GBP_TRACE("fft_z", st);
-    k<<<(unsigned)blocks, PAIRS * N / 16, smem, st>>>(mesh, spec, npen, tw);
-    GBP_LAUNCH_CHECK();
+    GBP_CUDA_TRY(launch_pdl(k, dim3((unsigned)blocks), dim3(PAIRS * N / 16), smem, st, mesh, spec, npen, tw));
   }
   const int nkb = P / C;
   const size_t smem = (size_t)fft::ColBlock<N, 1>::SLAB * sizeof(float2);
@@ -150,9 +150,8 @@ int run_fft(const float* mesh, float2* spec, int G, const float2* tw, cudaStream
   // x pass: a plane is one y row of one grid; rows (x) are N*P apart
   for (int g = 0; x_pass && g < G; ++g) {
     GBP_TRACE("fft_x", st);
-    kc<<<(unsigned)(N * nkb), N / 2, smem, st>>>(spec + (long long)g * N * N * P, P, (long long)N * P, N, nkb,
-                                                 tw);
-    GBP_LAUNCH_CHECK();
+    GBP_CUDA_TRY(launch_pdl(kc, dim3((unsigned)(N * nkb)), dim3(N / 2), smem, st, spec + (long long)g * N * N * P,
+                            (long long)P, (long long)N * P, N, nkb, tw));
   }
   return GBP_OK;
 }

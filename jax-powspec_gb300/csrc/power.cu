@@ -219,6 +219,7 @@ __device__ __forceinline__ void chunk1(const PowGeom& g, const Smem& s, float* w
 template <int NV, bool INTER, bool WIDE>
 __global__ void __launch_bounds__(POW_WARPS * 32, 4)
 power_kernel(PowGeom g) {
+  pdl_wait();
   extern __shared__ __align__(16) unsigned char smem[];
   const Smem s = load_tables<NV, INTER>(g, smem);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -350,14 +351,13 @@ int launch_power(const void* spectrum, int G, int Lzs, gbp_bins B, int mas_order
   const int grid = std::max(1, std::min(L.C, sms * std::max(per_sm, 1)));
   {
     GBP_TRACE("power_bins", stream);
-    kern<<<grid, L.warps * 32, L.smem, stream>>>(g);
-    GBP_LAUNCH_CHECK();
+    GBP_CUDA_TRY(launch_pdl(kern, dim3(grid), dim3(L.warps * 32), L.smem, stream, g));
   }
   GBP_TRACE("power_reduce", stream);
-  power_reduce_kernel<<<B->nb, FOLD_THREADS, 0, stream>>>(
-      part_ff, L.C, L.NV, B->nb, B->nbe, B->d_nmodes, B->d_ksum, sums_out, nmodes_out,
-      (ells & GBP_KSUM) ? ksum_out : nullptr);
-  GBP_LAUNCH_CHECK();
+  GBP_CUDA_TRY(launch_pdl(power_reduce_kernel, dim3(B->nb), dim3(FOLD_THREADS), 0, stream,
+                          static_cast<const float2*>(part_ff), L.C, L.NV, B->nb, B->nbe,
+                          static_cast<const long long*>(B->d_nmodes), static_cast<const double*>(B->d_ksum), sums_out,
+                          nmodes_out, (ells & GBP_KSUM) ? ksum_out : nullptr));
   return GBP_OK;
 }
 
