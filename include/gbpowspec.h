@@ -288,8 +288,13 @@ int gbp_fft_power(gbp_fft_plan plan, const float* mesh, void* spectrum,
  * interlaced); the column tile shape too (gbp_fft_plan_set_tiles).
  * Outputs as gbp_deposit (stats_out, required: it carries the mass the
  * binning and the normalisation use) followed by gbp_fft_power; `spectrum`
- * is scratch of the plan's spectrum size.  Replaces src/mas.py:88-153 +
- * src/correlations.py:7-56 for the production path. */
+ * is scratch of the plan's spectrum size.  The particles are bucketed by
+ * column tile in one pass into buckets of fixed capacity (twice the mean
+ * fill of a uniform catalogue of n_particles, plus 64); a catalogue that
+ * overflows one (a dense clump) is re-bucketed by a scan and a second pass
+ * in the same call, same results, GBP_STATS_REFILLED in stats_out->flags.
+ * Replaces src/mas.py:88-153 + src/correlations.py:7-56 for the production
+ * path. */
 int gbp_particles_power_workspace_size(int64_t n_particles, gbp_fft_plan plan,
                                        gbp_bins bins, int mas, int ells,
                                        size_t* bytes);
