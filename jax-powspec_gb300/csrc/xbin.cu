@@ -59,6 +59,7 @@ struct XLayout {
   static constexpr bool PAIRED = N >= 128;
   static constexpr int M2 = N / 128;
   static constexpr int MS2 = M2 < 8 ? M2 : 8;
+  static_assert(!PAIRED || (MS2 > 0 && M2 % MS2 == 0), "whole warp steps of mode pairs");
   static __host__ __device__ constexpr size_t data_bytes(int G) {
     const size_t rows = (size_t)G * fft::ColBlock<N, 2>::SLAB, cols = (size_t)G * XB_C * TST;
     return ((rows > cols ? rows : cols) * 8 + 127) & ~size_t(127);
